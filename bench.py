@@ -1,0 +1,439 @@
+"""Benchmark of the hot path: the 3-direction compact 4th-order derivative of
+a 512^3 FP64 field (3 x 262144 tridiagonal systems of length 512 per step),
+FP32 cyclic solves + double-word refinement (the headline path) beside the
+plain FP64 solve, on one GB300 per rank.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision P]
+    python bench.py --impl reference ...     # the reference's CPU path
+
+One JSON line on rank 0.  A step = dfdx, dfdy and dfdz of one field
+(experiments/run-compact.py:47-90), rows = 3 * 512^3 unknowns.  `value` is
+rows/s with the field resident in HBM (1 GiB input, larger than L2, so no
+flush is needed); `e2e` is the same through the public API with the field
+copied in from pinned host memory and the three derivatives copied back
+every step.  Multi-GPU: every rank solves its own field (independent
+replicas, no collective on the data path), value = all ranks' rows / the
+slowest rank's time.
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "near-toeplitz-applications_gb300")
+sys.path.insert(0, PKG_DIR)
+
+METRIC = "rows/s & HBM GB/s (frac of peak): FP64 vs FP32+refine at 1e-12 rel err"
+N = 512
+ROWS_PER_STEP = 3 * N ** 3
+BYTES_PER_ROW = 16  # read f (8 B) + write the derivative (8 B)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_tag):
+    """dram bytes per launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "%s.md" % kernel_tag)
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", text)
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        sm = []
+        mx = []
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx.append(float(s[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, val in zip(names, s[5:9]):
+                if val.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl != "reference" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def max_over_ranks(x, world, device=None):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world, device=None):
+    if world > 1:
+        import torch.distributed as dist
+
+        if device is not None and device.type == "cuda":
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# the reference's CPU path (experiments/run-compact.py:14-28: RHS in NumPy,
+# one banded LAPACK solve with every system as a right-hand-side column)
+# ---------------------------------------------------------------------------
+def _cpu_worker(task):
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
+    import oracle as O
+
+    axis, lines, seed = task
+    rng = np.random.default_rng(seed)
+    # `lines` complete lines of length N along `axis` from a 512^3 Fourier
+    # field sample: a [lines][N] slab built with the generator's modes
+    from ntk.workloads import fourier_modes
+
+    amps, ks, phases = fourier_modes(3, seed=0)
+    g = np.linspace(0, 1, N)
+    pos = rng.integers(0, N, size=(lines, 2)) / (N - 1)
+    f = np.zeros((lines, N))
+    for a, k, p in zip(amps, ks, phases):
+        kk = [float(v) for v in k]
+        other = [i for i in range(3) if i != axis]
+        arg = 2 * np.pi * (kk[axis] * g[None, :] + kk[other[0]] * pos[:, 0:1] + kk[other[1]] * pos[:, 1:2] + p)
+        f += a * np.sin(arg)
+    h = 1.0 / (N - 1)
+    t0 = time.perf_counter()
+    x = O.banded_compact_deriv(f.T.reshape(N, lines, 1), h, axis=0)
+    dt = time.perf_counter() - t0
+    return dt, lines * N, float(np.abs(x).sum())
+
+
+def cpu_path_rate(lines_per_task, tasks, processes):
+    """rows/s of the reference CPU path (RHS + banded solve, field generation
+    excluded) on `processes` concurrent worker processes: total rows over the
+    per-process solve time."""
+    import multiprocessing as mp
+
+    jobs = [((t % 3), lines_per_task, 1000 + t) for t in range(tasks)]
+    if processes == 1:
+        res = [_cpu_worker(j) for j in jobs]
+    else:
+        with mp.get_context("spawn").Pool(processes) as pool:
+            res = pool.map(_cpu_worker, jobs)
+    busy = sum(r[0] for r in res) / processes
+    rows = sum(r[1] for r in res)
+    return rows / busy, rows, busy
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    # warm-up: one small task per process (imports, LAPACK init)
+    cpu_path_rate(64, cores, cores)
+    lines = 4096  # 4096 lines x 512 rows per task
+    times = []
+    rows_total = 0
+    for _ in range(args.warmup):
+        cpu_path_rate(lines, cores, cores)
+    for _ in range(args.steps):
+        rate, rows, wall = cpu_path_rate(lines, cores, cores)
+        times.append(wall)
+        rows_total += rows
+    value = rows_total / sum(times)
+    ms_per_step = ROWS_PER_STEP / value * 1e3
+    line = {
+        "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "compact4 derivative x,y,z of a 512^3 FP64 field (3 x 262144 systems, n=512)",
+                   "precision": "fp64 (LAPACK banded solve)", "sample": "%d x %d lines of 512 per step" % (cores, lines)},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "rows/s", "cores": cores, "kind": "port",
+                         "sample": "%d tasks x %d systems of n=512 per step, numpy RHS + scipy solve_banded "
+                                   "(experiments/run-compact.py:14-28), %d processes" % (cores, lines, cores)},
+        "e2e": {"value": value, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# the GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+
+    import ntk
+    from ntk.workloads import COMPACT_COEFFS, fourier_field
+
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    h = 1.0 / (N - 1)
+    f = fourier_field((N, N, N), seed=rank, device=dev)
+    outs = [torch.empty_like(f) for _ in range(3)]
+    plans = {p: ntk.Plan(N, 0, COMPACT_COEFFS, precision=p, refine_sweeps=args.sweeps)
+             for p in ("fp64", "fp32", "fp32_refine")}
+    main = plans[args.precision]
+
+    def step(plan):
+        for axis in (2, 1, 0):
+            plan.compact_deriv(f, outs[2 - axis], axis=axis, h=h)
+
+    def timed(plan, steps, warmup, per_launch=False):
+        for _ in range(warmup):
+            step(plan)
+        torch.cuda.synchronize(dev)
+        barrier(world, dev)
+        torch.cuda.synchronize(dev)
+        ev = []
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            if per_launch:
+                for axis in (2, 1, 0):
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    plan.compact_deriv(f, outs[2 - axis], axis=axis, h=h)
+                    b.record(stream)
+                    ev.append((axis, a, b))
+            else:
+                step(plan)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier(world, dev)
+        ms = e0.elapsed_time(e1) / steps
+        per = {}
+        for axis, a, b in ev:
+            per.setdefault(axis, []).append(a.elapsed_time(b))
+        return ms, {ax: sum(v) / len(v) for ax, v in per.items()}
+
+    # accuracy (rank 0): refine and FP32 against the FP64 solve, and the
+    # FP64 solve against the FP64 banded oracle on sampled lines
+    errs = {}
+    if rank == 0:
+        ref = [torch.empty_like(f) for _ in range(3)]
+        for axis in (2, 1, 0):
+            plans["fp64"].compact_deriv(f, ref[2 - axis], axis=axis, h=h)
+        for p in ("fp32", "fp32_refine"):
+            m = 0.0
+            for axis in (2, 1, 0):
+                plans[p].compact_deriv(f, outs[2 - axis], axis=axis, h=h)
+                m = max(m, float((outs[2 - axis] - ref[2 - axis]).abs().max() / ref[2 - axis].abs().max()))
+            errs[p + "_vs_fp64"] = m
+        errs.update(sample_oracle_errors(f, ref, h))
+        del ref
+        torch.cuda.empty_cache()
+
+    # device-resident timing: headline path, per-launch events for the roofline
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_main, _ = timed(main, args.steps, args.warmup)
+    clocks.stop()
+    _, per_axis = timed(main, max(2, args.steps // 2), 1, per_launch=True)
+    ms_fp64, per_axis64 = timed(plans["fp64"], max(2, args.steps // 2), 1, per_launch=True)
+    ms_fp32, _ = timed(plans["fp32"], max(2, args.steps // 2), 1)
+    ms_main = max_over_ranks(ms_main, world, dev)
+    ms_fp64 = max_over_ranks(ms_fp64, world, dev)
+
+    # end to end through the public API: pinned host f in, three derivatives out
+    hf = torch.empty((N, N, N), dtype=torch.float64, pin_memory=True)
+    hf.copy_(f)
+    houts = [torch.empty((N, N, N), dtype=torch.float64, pin_memory=True) for _ in range(3)]
+    fd = torch.empty_like(f)
+
+    def e2e_step():
+        fd.copy_(hf, non_blocking=True)
+        for axis in (2, 1, 0):
+            main.compact_deriv(fd, outs[2 - axis], axis=axis, h=h)
+        for i in range(3):
+            houts[i].copy_(outs[i], non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize(dev)
+    barrier(world, dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    e2e_steps = max(2, args.steps // 2)
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms_e2e = max_over_ranks(e0.elapsed_time(e1) / e2e_steps, world, dev)
+
+    if rank != 0:
+        return 0
+    hbm, peak_kind = peaks()
+    rows_launch = N ** 3
+    alg_bytes_launch = BYTES_PER_ROW * rows_launch
+    dominant_axis = max(per_axis, key=lambda a: per_axis[a])
+    launch_ms = per_axis[dominant_axis]
+    achieved = alg_bytes_launch / (launch_ms * 1e-3) / 1e9
+    value = world * ROWS_PER_STEP / (ms_main * 1e-3)
+    traffic = profile_traffic("refine_kernel_512cube" if args.precision != "fp64" else "thomas_f64_512cube")
+    cpu = None
+    if not args.no_cpu_baseline:
+        rate, rows, wall = cpu_path_rate(4096, 24, 1)
+        cpu = {"value": rate, "unit": "rows/s", "cores": 1, "kind": "port",
+               "sample": "%d systems of n=512 (x, y, z lines of the 512^3 field), numpy RHS + scipy "
+                         "solve_banded (experiments/run-compact.py:14-28), 1 process, %.1f s" % (rows // N, wall)}
+    line = {
+        "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_main, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": {"fp64": "f64", "fp32": "f32 (f64 in/out)",
+                  "fp32_refine": "f32 solve + double-word (2x f32) residual/accumulate, f64 in/out"}[args.precision],
+        "data": "synthetic",
+        "config": {"workload": "compact4 derivative x,y,z of a 512^3 FP64 field (3 x 262144 systems, n=512)",
+                   "precision": args.precision, "refine_sweeps": args.sweeps,
+                   "l2": "1 GiB input > 129 MB L2 (no flush)", "parallelism": "replicas x%d" % world},
+        "fp64": {"ms_per_step": ms_fp64, "rows_per_s": world * ROWS_PER_STEP / (ms_fp64 * 1e-3),
+                 "hbm_frac": (BYTES_PER_ROW * N ** 3 / (per_axis64[max(per_axis64, key=per_axis64.get)] * 1e-3) / 1e9)
+                 / hbm},
+        "fp32_only": {"ms_per_step": ms_fp32, "rows_per_s": world * ROWS_PER_STEP / (ms_fp32 * 1e-3)},
+        "speedup_vs_fp64": ms_fp64 / ms_main,
+        "errors": errs,
+        "per_axis_ms": {"x": per_axis.get(2), "y": per_axis.get(1), "z": per_axis.get(0)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "%s, axis %s, %d rows x 16 B per launch" % (
+                         "refine_kernel" if args.precision != "fp64" else "thomas_f64_kernel",
+                         "xyz"[2 - dominant_axis], rows_launch)},
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * ROWS_PER_STEP / (ms_e2e * 1e-3), "unit": "rows/s",
+                "h2d_bytes_per_step": 8 * N ** 3, "d2h_bytes_per_step": 3 * 8 * N ** 3},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    for p in plans.values():
+        p.close()
+    return 0
+
+
+def sample_oracle_errors(f, ref, h, lines=256):
+    """FP64 GPU derivative vs the FP64 banded oracle on sampled lines."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
+    import oracle as O
+
+    rng = np.random.default_rng(7)
+    worst = 0.0
+    fc = f
+    for axis in (2, 1, 0):
+        idx = rng.integers(0, N, size=(lines, 2))
+        if axis == 2:
+            fl = fc[idx[:, 0], idx[:, 1], :]
+            rl = ref[0][idx[:, 0], idx[:, 1], :]
+        elif axis == 1:
+            fl = fc[idx[:, 0], :, idx[:, 1]]
+            rl = ref[1][idx[:, 0], :, idx[:, 1]]
+        else:
+            fl = fc[:, idx[:, 0], idx[:, 1]].T
+            rl = ref[2][:, idx[:, 0], idx[:, 1]].T
+        fl = fl.cpu().numpy()
+        rl = rl.cpu().numpy()
+        x = O.banded_compact_deriv(fl[:, None, :], h, axis=2)[:, 0, :]
+        worst = max(worst, O.rel_err(rl, x))
+    return {"fp64_vs_banded_oracle": worst}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ntk", choices=["ntk", "reference"])
+    ap.add_argument("--precision", default="fp32_refine", choices=["fp64", "fp32", "fp32_refine"])
+    ap.add_argument("--sweeps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

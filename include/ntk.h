@@ -1,0 +1,170 @@
+/*
+ * ntk.h -- C ABI of libntk, the GB300-native (sm_103a) batched near-Toeplitz
+ * tridiagonal solver with the compact finite-difference and ADI operators
+ * around it.
+ *
+ * Drop-in boundary for the hot path of ashwinsrnth/near-toeplitz-applications:
+ * plain pointers and sizes, no C++ or torch types.  Device pointers are CUDA
+ * device addresses of the calling process's current device; `stream` is a
+ * cudaStream_t (NULL = legacy default stream, as the reference uses).  Every
+ * call is asynchronous with respect to the host unless stated otherwise and
+ * returns an ntk_status; ntk_last_error() returns the message of the last
+ * failure on the calling thread.
+ *
+ * Matrices follow the reference's model (neato.py:131-139): coeffs =
+ * (b1, c1, ai, bi, ci, an, bn), row 0 = [b1 c1], rows 1..n-2 = [ai bi ci],
+ * row n-1 = [an bn].  n >= 3; unlike the reference, n need not be a power
+ * of two and is not capped at 2048.
+ */
+#ifndef NTK_H
+#define NTK_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ntk_status {
+  NTK_OK = 0,
+  NTK_ERR_INVALID = 1,     /* bad argument (size, pointer, stride, mode) */
+  NTK_ERR_CUDA = 2,        /* a CUDA runtime call or launch failed */
+  NTK_ERR_UNSUPPORTED = 3, /* valid request this build does not serve */
+  NTK_ERR_RANGE = 4,       /* input magnitude outside the FP32+refine range */
+  NTK_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  NTK_ERR_ALLOC = 6        /* host or device allocation failed */
+} ntk_status;
+
+typedef enum ntk_precision {
+  NTK_FP64 = 0,            /* plain FP64 solve */
+  NTK_FP32 = 1,            /* FP32 solve only (no refinement) */
+  NTK_FP32_REFINE = 2      /* FP32 solves + double-word residual refinement */
+} ntk_precision;
+
+typedef struct ntk_plan ntk_plan;
+
+/* Version string of the library build. */
+const char* ntk_version(void);
+
+/* Message of the last failed call on this thread ("" if none).  Copies at
+ * most len-1 bytes plus a terminating NUL into buf; returns the full length. */
+int ntk_last_error(char* buf, int len);
+
+/* Builds a solver for systems of length n with the reference's coefficient
+ * tuple.  Replaces NearToeplitzSolver.__init__ (neato.py:131-166): the
+ * per-level CR coefficient arrays of _precompute_coefficients
+ * (neato.py:199-274) become the shared matrix's LU factors, computed once in
+ * FP64 on the host and uploaded.  nrhs is the number of contiguous systems
+ * ntk_solve works on (neato.py:135-136).  precision is an ntk_precision;
+ * refine_sweeps (>= 1) is used by NTK_FP32_REFINE.  Synchronous. */
+int ntk_plan_create(ntk_plan** out, int n, long long nrhs, const double coeffs[7], int precision,
+                    int refine_sweeps);
+
+/* Frees the plan's device tables.  Synchronous; NULL is accepted. */
+int ntk_plan_destroy(ntk_plan* plan);
+
+/* Solves plan->nrhs contiguous systems in place: d[s*n + k], 0 <= s < nrhs.
+ * Replaces NearToeplitzSolver.solve(x_d) (neato.py:168-197); d may be a
+ * pointer-offset view into a larger buffer, as in experiments/run-adi.py:65. */
+int ntk_solve(ntk_plan* plan, double* d, void* stream);
+
+/* Solves nsys systems laid out with strides (in elements): system s starts at
+ * (s / ni) * os + (s % ni) * is and its k-th unknown is es further on per k.
+ * The y and z sweeps of a C-ordered [nz][ny][nx] field are
+ *   y: ni = nx, is = 1, os = nx*ny, es = nx      (nsys = nz*nx)
+ *   z: ni = nx*ny, is = 1, os = 0, es = nx*ny    (nsys = ny*nx)
+ * which removes the permutes of experiments/run-compact.py:70-73,83-86.
+ * In place (d_out == d_in) or out of place with the same layout. */
+int ntk_solve_strided(ntk_plan* plan, const double* d_in, double* d_out, long long nsys, long long ni,
+                      long long is, long long os, long long es, void* stream);
+
+/* Compact 4th-order first derivative of an [nz][ny][nx] FP64 field along
+ * axis (0 = z, 1 = y, 2 = x), grid spacing h: the RHS of compact/rhs.py:9-37
+ * fused into the solve's load phase, with strided addressing for y and z.
+ * Replaces compute_rhs + solve (experiments/run-compact.py:57-60) and, for
+ * y/z, the two permutes around them (run-compact.py:67-90).  The plan's n
+ * must equal the extent of the chosen axis; nrhs is ignored.  out must not
+ * overlap f unless out == f. */
+int ntk_compact_deriv(ntk_plan* plan, const double* f, double* out, int nz, int ny, int nx, int axis, double h,
+                      void* stream);
+
+/* compute_rhs(f, rhs, dx) of compact/rhs.py:47-53: the RHS along the last
+ * axis of an [nz][ny][nx] field.  Any nz, ny >= 1 and nx >= 3 (the
+ * reference needs multiples of 8). */
+int ntk_compact_rhs(const double* f, double* rhs, int nz, int ny, int nx, double dx, void* stream);
+
+/* permute(a_d, b_d, permutation) of compact/permute.py:32-52:
+ * out[i0][i1][i2] = in[i0*s0 + i1*s1 + i2*s2] with out of shape (o0, o1, o2)
+ * and (s0, s1, s2) the input's element strides in permutation order. */
+int ntk_permute3d(const double* in, double* out, int o0, int o1, int o2, long long s0, long long s1, long long s2,
+                  void* stream);
+
+/* compute_rhs(u, d, dx, dt, N) of adi/rhs.py:35-55: interior points of d get
+ * bottom*u[i-N] + center*u[i] + top*u[i+N] with the reference's dx, dt
+ * coefficients (adi/rhs.py:46-49); boundary points of d are untouched. */
+int ntk_adi_rhs(const double* u, double* d, int N, double dx, double dt, void* stream);
+
+/* transpose(a, b, N) of adi/transpose.py:40-50: b = a^T for N x N FP64. */
+int ntk_transpose2d(const double* a, double* b, int N, void* stream);
+
+/* ---- ADI (Peaceman-Rachford) heat equation on an N x N grid ------------
+ * One step replaces the six launches of experiments/run-adi.py:59-71
+ * (compute_rhs, solve, transpose, twice) with two fused half steps and no
+ * transpose.  The matrix is the reference's (run-adi.py:50-53):
+ * (1, 0, 1/dx^2, -2(1/dt + 1/dx^2), 1/dx^2, 0, 1), RHS stencil adi/rhs.py:46-49. */
+typedef struct ntk_adi ntk_adi;
+
+/* Builds the ADI solver for N x N fields (N >= 4).  precision: NTK_FP64.
+ * Allocates an N x N FP64 work array.  Synchronous. */
+int ntk_adi_create(ntk_adi** out, int N, double dx, double dt, int precision);
+
+int ntk_adi_destroy(ntk_adi* adi);
+
+/* The segmentation the plan chose: segment length, halo and segments per
+ * system of the FP64 sweeps (1 segment = plain sweeps). */
+int ntk_adi_segments(const ntk_adi* adi, int* seg_len, int* halo, int* nseg);
+
+/* One time step on device arrays u, d_x, d_y (N x N, C order), with the
+ * reference's meaning: afterwards u is the reference's u after one loop
+ * iteration and rows 1..N-2 of d_x hold the x half step's solution.  d_y is
+ * read only at its boundary columns (0 and N-1 of rows 1..N-2); its interior,
+ * scratch in the reference, is not written.  u's boundary columns are not
+ * rewritten: with the reference's initialisation d_y = u^T
+ * (run-adi.py:45-46) they already hold the values the reference's last
+ * transpose would put there. */
+int ntk_adi_step(ntk_adi* adi, double* u, double* d_x, const double* d_y, void* stream);
+
+/* `steps` time steps.  use_graph != 0 captures the steps once per
+ * (u, d_x, d_y, steps) into a CUDA graph and replays it on later calls. */
+int ntk_adi_run(ntk_adi* adi, double* u, double* d_x, const double* d_y, int steps, int use_graph, void* stream);
+
+/* ---- uneven batches ------------------------------------------------------
+ * nsys independent near-Toeplitz systems of different lengths and
+ * coefficients in one buffer, solved in place by one persistent launch.
+ * Generalises NearToeplitzSolver (neato.py:129-197: one matrix, one
+ * power-of-two n <= 2048) to a descriptor table.  System s: n[s] >= 3 rows
+ * starting at element offset[s]; interior rows (a, b, c) =
+ * interior[3s .. 3s+2]; rows 0 and 1 = head[6s .. 6s+5] as (a, b, c) pairs
+ * (a of row 0 ignored); rows n-2 and n-1 = tail[6s .. 6s+5] (c of row n-1
+ * ignored).  Systems must not overlap. */
+typedef struct ntk_batch ntk_batch;
+
+/* Factors every system on the host (FP64) and uploads the tables; allocates
+ * a work array as large as the data buffer.  precision: NTK_FP64.
+ * Synchronous. */
+int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long long* offset, const double* interior,
+                     const double* head, const double* tail, int precision);
+
+int ntk_batch_destroy(ntk_batch* batch);
+
+/* Longest system, number of systems split over several lanes, and the
+ * number of elements the data buffer must span. */
+int ntk_batch_info(const ntk_batch* batch, long long* max_n, long long* segmented, long long* elements);
+
+/* Solves every system in place in d (device).  One kernel launch preceded
+ * by a 4-byte memset of the work counter on the same stream. */
+int ntk_batch_solve(ntk_batch* batch, double* d, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NTK_H */

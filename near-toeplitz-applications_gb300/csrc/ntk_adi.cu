@@ -1,0 +1,248 @@
+// ntk_adi.cu -- Peaceman-Rachford ADI time step (experiments/run-adi.py:59-71).
+//
+// The reference runs six kernels per step: vertical stencil, row solve,
+// transpose, vertical stencil, row solve, transpose (adi/rhs.py:10-25,
+// neato.py:8-124, adi/transpose.py:9-27).  Here a step is two fused half
+// steps and no transpose:
+//   x half: systems = rows 1..N-2 of d_x; RHS = the vertical stencil of u
+//           (rows j-1, j, j+1), boundary RHS = d_x's own boundary columns;
+//           result written to d_x (as the reference's solve does).
+//   y half: systems = columns 1..N-2 of d_x, solved with strided addressing;
+//           RHS = the stencil of d_x along its rows (the reference's
+//           vertical stencil of u = d_x^T), boundary RHS = d_y's boundary
+//           columns; result written straight into u's column, which is
+//           where the reference's final transpose puts it.
+// Each half step uses the segmented FP64 sweeps (ntk_solve_f64.cu) when the
+// factors decay fast enough for the halo to be exact to rounding (r = 0.5:
+// |l| -> 0.268, a 34-row halo), giving 2046 x 8 threads instead of 2046.
+// A whole run of steps can be captured once in a CUDA graph and replayed.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "ntk_internal.h"
+#include "ntk_plan.h"
+
+namespace ntk {
+
+struct Adi {
+  int N = 0;
+  double dx = 0, dt = 0;
+  int precision = NTK_FP64;
+  Plan plan;
+  double* scratch = nullptr;  // N x N forward values of the segmented sweeps
+  SegParams sp;
+  double bottom = 0, center = 0, top = 0;
+  cudaStream_t capture_stream = nullptr;
+  std::map<std::tuple<const void*, const void*, const void*, int>, cudaGraphExec_t> graphs;
+
+  ~Adi() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+    if (scratch) cudaFree(scratch);
+  }
+};
+
+namespace {
+
+// Smallest halo H such that every forward window [gL-H, gL) and backward
+// window [(g+1)L, (g+1)L+H) has a factor product below 2^-64.
+SegParams choose_segments(const std::vector<double>& l, const std::vector<double>& w, int n, long long nsys) {
+  SegParams sp;
+  sp.P = 1;
+  sp.L = n;
+  sp.H = 0;
+  // enough threads to cover the GPU several times over
+  int P = 1;
+  while (nsys * P < 152LL * 96 && P < 64 && n / (2 * P) >= 64) P *= 2;
+  if (P == 1) return sp;
+  const int L = (n + P - 1) / P;
+  const double lim = std::ldexp(1.0, -64);
+  for (int H = 8; H <= L / 2; H += 2) {
+    bool ok = true;
+    for (int g = 1; g < P && ok; ++g) {
+      double prod = 1.0;
+      for (int i = std::max(1, g * L - H); i < g * L; ++i) prod *= std::fabs(l[i]);
+      ok = prod <= lim;
+    }
+    for (int g = 0; g < P - 1 && ok; ++g) {
+      double prod = 1.0;
+      const int e = std::min(n, (g + 1) * L);
+      for (int i = e; i < std::min(n, e + H); ++i) prod *= std::fabs(w[i - 1]);
+      ok = prod <= lim;
+    }
+    if (ok) {
+      sp.P = P;
+      sp.L = L;
+      sp.H = H;
+      return sp;
+    }
+  }
+  return sp;
+}
+
+}  // namespace
+
+int adi_step(Adi* a, double* u, double* d_x, const double* d_y, cudaStream_t st) {
+  const int N = a->N;
+  TablesF64 t;
+  t.l = a->plan.d_lw;
+  t.w = a->plan.d_lw + N;
+  int rc = a->plan.g_table(1.0, &t.g);
+  if (rc) return rc;
+  // x half step
+  Batch bx;
+  bx.nsys = N - 2;
+  bx.ni = N - 2;
+  bx.is = N;
+  bx.os = 0;
+  bx.es = 1;
+  RhsParams rx;
+  rx.kind = RHS_CROSS;
+  rx.bottom = a->bottom;
+  rx.center = a->center;
+  rx.top = a->top;
+  rx.cs = N;
+  rx.bnd = d_x + N;
+  rx.bnd_ss = N;
+  rx.bnd_es = 1;
+  rc = launch_thomas_f64_segmented(u + N, a->scratch + N, d_x + N, N, bx, rx, t, a->sp, st);
+  if (rc) return rc;
+  // y half step
+  Batch by;
+  by.nsys = N - 2;
+  by.ni = N - 2;
+  by.is = 1;
+  by.os = 0;
+  by.es = N;
+  RhsParams ry = rx;
+  ry.cs = 1;
+  ry.bnd = d_y + N;
+  ry.bnd_ss = N;
+  ry.bnd_es = 1;
+  return launch_thomas_f64_segmented(d_x + 1, a->scratch + 1, u + 1, N, by, ry, t, a->sp, st);
+}
+
+}  // namespace ntk
+
+struct ntk_adi : public ntk::Adi {};
+
+extern "C" {
+
+int ntk_adi_create(ntk_adi** out, int N, double dx, double dt, int precision) {
+  if (!out) {
+    ntk::set_error("ntk_adi_create: null out");
+    return NTK_ERR_INVALID;
+  }
+  *out = nullptr;
+  if (N < 4 || !(dx > 0) || !(dt > 0) || !std::isfinite(dx) || !std::isfinite(dt)) {
+    ntk::set_error("ntk_adi_create: need N >= 4 and positive finite dx, dt");
+    return NTK_ERR_INVALID;
+  }
+  if (precision != NTK_FP64) {
+    ntk::set_error("ntk_adi_create: this build runs ADI in NTK_FP64 only");
+    return NTK_ERR_UNSUPPORTED;
+  }
+  ntk_adi* a = new (std::nothrow) ntk_adi();
+  if (!a) {
+    ntk::set_error("ntk_adi_create: out of host memory");
+    return NTK_ERR_ALLOC;
+  }
+  a->N = N;
+  a->dx = dx;
+  a->dt = dt;
+  a->precision = precision;
+  // experiments/run-adi.py:50-53 and adi/rhs.py:46-49
+  const double co[7] = {1., 0., 1. / (dx * dx), -2. * (1. / dt + 1. / (dx * dx)), 1. / (dx * dx), 0., 1.};
+  a->bottom = -1. / (dx * dx);
+  a->top = -1. / (dx * dx);
+  a->center = 2 * (-1. / dt + 1. / (dx * dx));
+  int rc = a->plan.init(N, N - 2, co, NTK_FP64, 1);
+  if (rc == NTK_OK) {
+    std::vector<double> w(N);
+    for (int i = 0; i < N; ++i) w[i] = (i < N - 1 ? a->plan.mat.c(i) : 0.0) / a->plan.lu_u[i];
+    a->sp = ntk::choose_segments(a->plan.lu_l, w, N, N - 2);
+    rc = ntk::cuda_status(cudaMalloc(&a->scratch, sizeof(double) * (size_t)N * N), "cudaMalloc(ADI scratch)");
+  }
+  if (rc) {
+    delete a;
+    return rc;
+  }
+  *out = a;
+  return NTK_OK;
+}
+
+int ntk_adi_destroy(ntk_adi* adi) {
+  delete adi;
+  return NTK_OK;
+}
+
+int ntk_adi_segments(const ntk_adi* adi, int* seg_len, int* halo, int* nseg) {
+  if (!adi) {
+    ntk::set_error("ntk_adi_segments: null plan");
+    return NTK_ERR_INVALID;
+  }
+  if (seg_len) *seg_len = adi->sp.L;
+  if (halo) *halo = adi->sp.H;
+  if (nseg) *nseg = adi->sp.P;
+  return NTK_OK;
+}
+
+int ntk_adi_step(ntk_adi* adi, double* u, double* d_x, const double* d_y, void* stream) {
+  if (!adi || !u || !d_x || !d_y) {
+    ntk::set_error("ntk_adi_step: null argument");
+    return NTK_ERR_INVALID;
+  }
+  int rc = adi->plan.check_device();
+  if (rc) return rc;
+  return ntk::adi_step(adi, u, d_x, d_y, (cudaStream_t)stream);
+}
+
+int ntk_adi_run(ntk_adi* adi, double* u, double* d_x, const double* d_y, int steps, int use_graph, void* stream) {
+  if (!adi || !u || !d_x || !d_y || steps < 0) {
+    ntk::set_error("ntk_adi_run: bad argument");
+    return NTK_ERR_INVALID;
+  }
+  int rc = adi->plan.check_device();
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!use_graph) {
+    for (int s = 0; s < steps; ++s)
+      if ((rc = ntk::adi_step(adi, u, d_x, d_y, st))) return rc;
+    return NTK_OK;
+  }
+  auto key = std::make_tuple((const void*)u, (const void*)d_x, (const void*)d_y, steps);
+  auto it = adi->graphs.find(key);
+  if (it == adi->graphs.end()) {
+    // make sure the g table exists before capture (it is uploaded synchronously)
+    const double* g = nullptr;
+    if ((rc = adi->plan.g_table(1.0, &g))) return rc;
+    if (!adi->capture_stream) {
+      rc = ntk::cuda_status(cudaStreamCreateWithFlags(&adi->capture_stream, cudaStreamNonBlocking),
+                            "cudaStreamCreate(capture)");
+      if (rc) return rc;
+    }
+    rc = ntk::cuda_status(cudaStreamBeginCapture(adi->capture_stream, cudaStreamCaptureModeThreadLocal),
+                          "cudaStreamBeginCapture");
+    if (rc) return rc;
+    int lrc = NTK_OK;
+    for (int s = 0; s < steps && lrc == NTK_OK; ++s) lrc = ntk::adi_step(adi, u, d_x, d_y, adi->capture_stream);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(adi->capture_stream, &graph);
+    if (lrc) {
+      if (graph) cudaGraphDestroy(graph);
+      return lrc;
+    }
+    if ((rc = ntk::cuda_status(e, "cudaStreamEndCapture"))) return rc;
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if ((rc = ntk::cuda_status(e, "cudaGraphInstantiate"))) return rc;
+    it = adi->graphs.emplace(key, exec).first;
+  }
+  return ntk::cuda_status(cudaGraphLaunch(it->second, st), "cudaGraphLaunch");
+}
+
+}  // extern "C"

@@ -1,0 +1,82 @@
+// ntk_internal.h -- host-side declarations shared by the ntk translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+
+#include "../../include/ntk.h"
+
+namespace ntk {
+
+// How a batch of systems sits in memory: system s (0 <= s < nsys) starts at
+// element (s / ni) * os + (s % ni) * is and its k-th unknown is at
+// start + k * es.  Every direction of a C-ordered [nz][ny][nx] field is one
+// of these without copies:
+//   x: ni = nsys, is = nx, es = 1
+//   y: ni = nx, is = 1, os = nx*ny, es = nx
+//   z: ni = nx*ny, is = 1, es = nx*ny
+struct Batch {
+  long long nsys = 0;
+  long long ni = 1;
+  long long is = 0;
+  long long os = 0;
+  long long es = 1;
+};
+
+// Right-hand side applied inside the solve's load phase.
+enum RhsKind : int {
+  RHS_IDENTITY = 0,  // d is given (in place solve)
+  RHS_COMPACT = 1,   // compact 4th-order first derivative of f along the system
+  RHS_CROSS = 2,     // 3-point stencil across systems (ADI explicit half)
+};
+
+// Parameters of the fused right-hand sides, in the units the kernels use:
+// the solve is carried out on eta = y / s (s the interior RHS scale) so the
+// interior RHS needs no multiply.
+struct RhsParams {
+  int kind = RHS_IDENTITY;
+  double sigma0 = 1.0;  // boundary-row scale, row 0   (compact: s_0 / s)
+  double sigmaN = 1.0;  // boundary-row scale, row n-1
+  // cross stencil: d_i = bottom * in[i - cs] + center * in[i] + top * in[i + cs]
+  double bottom = 0, center = 0, top = 0;
+  long long cs = 0;             // element offset of the stencil's neighbours across systems
+  const double* bnd = nullptr;  // boundary-row values D_0, D_{n-1} (cross stencil)
+  long long bnd_ss = 0;         // boundary values of system s start at bnd + s * bnd_ss
+  long long bnd_es = 1;         // D_{n-1} is at (n-1) * bnd_es from D_0
+};
+
+// Decay-truncated segmentation of the Thomas sweeps: system s is cut into P
+// segments of L rows; the forward sweep of segment g starts H rows early
+// from zero and the backward sweep H rows late from zero.  Used only when
+// the products of |l_i| (|w_i|) over every halo window are below 2^-64, so
+// the truncation is below FP64 rounding.
+struct SegParams {
+  int L = 0;
+  int H = 0;
+  int P = 1;
+};
+
+// FP64 factor tables of the shared matrix (length n each), device memory.
+struct TablesF64 {
+  const double* l = nullptr;  // l_i = a_i / u_{i-1}
+  const double* g = nullptr;  // g_i = s / u_i
+  const double* w = nullptr;  // w_i = c_i / u_i
+};
+
+void set_error(const char* fmt, ...);
+int cuda_status(cudaError_t e, const char* where);
+
+// kernels (ntk_solve_f64.cu)
+int launch_thomas_f64(const double* in, double* out, int n, const Batch& b, const RhsParams& rp,
+                      const TablesF64& t, int threads, cudaStream_t stream);
+int launch_thomas_f64_segmented(const double* in, double* eta, double* out, int n, const Batch& b,
+                                const RhsParams& rp, const TablesF64& t, const SegParams& sp, cudaStream_t stream);
+
+// standalone operators (ntk_ops.cu)
+int launch_compact_rhs(const double* f, double* rhs, int nz, int ny, int nx, double dx, cudaStream_t s);
+int launch_permute3d(const double* in, double* out, int o0, int o1, int o2, long long s0, long long s1,
+                     long long s2, cudaStream_t s);
+int launch_adi_rhs(const double* u, double* d, int N, double bottom, double center, double top, cudaStream_t s);
+int launch_transpose2d(const double* a, double* b, int N, cudaStream_t s);
+
+}  // namespace ntk

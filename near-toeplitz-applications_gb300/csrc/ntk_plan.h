@@ -1,0 +1,85 @@
+// ntk_plan.h -- the solver plan behind the opaque ntk_plan handle.
+#pragma once
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "ntk_internal.h"
+
+#define NTK_STR2(x) #x
+#define NTK_STR(x) NTK_STR2(x)
+
+namespace ntk {
+
+// A near-Toeplitz tridiagonal matrix: up to two special rows at each end,
+// constant (ai, bi, ci) in between.  The reference's model (neato.py:136-138)
+// is one special row at each end.
+struct Matrix {
+  int n = 0;
+  int nh = 1, nt = 1;                          // special rows at head / tail
+  double ha[2] = {0, 0}, hb[2] = {1, 1}, hc[2] = {0, 0};
+  double ta[2] = {0, 0}, tb[2] = {1, 1}, tc[2] = {0, 0};
+  double ai = 0, bi = 1, ci = 0;
+
+  void set_reference(const double co[7]) {
+    nh = nt = 1;
+    ha[0] = 0.0;
+    hb[0] = co[0];
+    hc[0] = co[1];
+    ai = co[2];
+    bi = co[3];
+    ci = co[4];
+    ta[0] = co[5];
+    tb[0] = co[6];
+    tc[0] = 0.0;
+  }
+  double a(int i) const {
+    if (i == 0) return 0.0;
+    if (i < nh) return ha[i];
+    if (i >= n - nt) return ta[i - (n - nt)];
+    return ai;
+  }
+  double b(int i) const {
+    if (i < nh) return hb[i];
+    if (i >= n - nt) return tb[i - (n - nt)];
+    return bi;
+  }
+  double c(int i) const {
+    if (i == n - 1) return 0.0;
+    if (i < nh) return hc[i];
+    if (i >= n - nt) return tc[i - (n - nt)];
+    return ci;
+  }
+};
+
+bool factor_host(const Matrix& m, std::vector<double>& l, std::vector<double>& u);
+
+struct RefineState;  // ntk_refine.cu
+
+struct Plan {
+  int n = 0;
+  long long nrhs = 0;
+  double coeffs[7] = {0, 0, 0, 0, 0, 0, 0};
+  Matrix mat;
+  int precision = NTK_FP64;
+  int sweeps = 1;
+  int device = -1;
+  std::vector<double> lu_l, lu_u;   // host LU factors (FP64)
+  double* d_lw = nullptr;           // device: l[n], w[n]
+  std::map<double, double*> g_by_scale;  // device g = s/u per RHS scale
+  RefineState* refine = nullptr;
+  std::mutex mu;
+
+  int init(int n, long long nrhs, const double co[7], int precision, int sweeps);
+  ~Plan();
+  int g_table(double s, const double** out);
+  int check_device() const;
+  int run(const double* in, double* out, const Batch& b, RhsParams rp, double s, cudaStream_t stream);
+
+  // FP32 / FP32 + refinement (ntk_refine.cu)
+  int init_refine();
+  int run_refine(const double* in, double* out, const Batch& b, const RhsParams& rp, double s, cudaStream_t stream);
+  void release_refine();
+};
+
+}  // namespace ntk

@@ -1,0 +1,140 @@
+// ntk_refine.cu -- host side of the FP32 / FP32+refinement path: FP32
+// factor tables in the padded chunk layout, dispatch to the kernel
+// instances (ntk_refine_m*.cu, kernel in ntk_refine.cuh).
+#include <cmath>
+#include <vector>
+
+#include "ntk_refine.cuh"
+
+namespace ntk {
+
+struct RefineState {
+  int M = 0;
+  int n_pad = 0;
+  float* d_tab = nullptr;
+  unsigned* d_status = nullptr;
+  bool pow2 = false;
+};
+
+namespace {
+
+DW to_dw(double v) {
+  DW d;
+  d.h = (float)v;
+  d.l = (float)(v - (double)d.h);
+  return d;
+}
+
+bool is_pow2_or_zero(double v) {
+  if (v == 0.0) return true;
+  int e;
+  double m = std::frexp(std::fabs(v), &e);
+  return m == 0.5 && e > -100 && e < 100;
+}
+
+}  // namespace
+
+int Plan::init_refine() {
+  RefineState* st = new (std::nothrow) RefineState();
+  if (!st) {
+    set_error("out of host memory");
+    return NTK_ERR_ALLOC;
+  }
+  refine = st;
+  int M = 0;
+  for (int m : {2, 4, 8, 16, 32})
+    if (n <= 32 * m) {
+      M = m;
+      break;
+    }
+  if (M == 0) {
+    set_error("FP32/refine precision supports n <= 1024 in this build (got %d); use NTK_FP64", n);
+    return NTK_ERR_UNSUPPORTED;
+  }
+  st->M = M;
+  st->n_pad = 32 * M;
+  // FP32 factor tables in the padded chunk layout; rows >= n are identity
+  std::vector<float> tab(3 * 32 * (M + 1), 0.f);
+  for (int r = 0; r < 32 * M; ++r) {
+    const int j = r / M, k = r % M;
+    float l = 0.f, g = 1.f, w = 0.f;
+    if (r < n) {
+      l = (float)lu_l[r];
+      g = (float)(1.0 / lu_u[r]);
+      w = (float)((r < n - 1 ? mat.c(r) : 0.0) / lu_u[r]);
+    }
+    tab[0 * 32 * (M + 1) + j * (M + 1) + k] = l;
+    tab[1 * 32 * (M + 1) + j * (M + 1) + k] = g;
+    tab[2 * 32 * (M + 1) + j * (M + 1) + k] = w;
+  }
+  int rc = cuda_status(cudaMalloc(&st->d_tab, tab.size() * sizeof(float)), "cudaMalloc(refine tables)");
+  if (rc) return rc;
+  rc = cuda_status(cudaMemcpy(st->d_tab, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice),
+                   "cudaMemcpy(refine tables)");
+  if (rc) return rc;
+  rc = cuda_status(cudaMalloc(&st->d_status, sizeof(unsigned)), "cudaMalloc(status)");
+  if (rc) return rc;
+  rc = cuda_status(cudaMemset(st->d_status, 0, sizeof(unsigned)), "cudaMemset(status)");
+  if (rc) return rc;
+  bool p2 = true;
+  for (int i = 0; i < n; ++i) {
+    p2 = p2 && is_pow2_or_zero(mat.a(i)) && is_pow2_or_zero(mat.b(i)) && is_pow2_or_zero(mat.c(i));
+  }
+  st->pow2 = p2;
+  return NTK_OK;
+}
+
+void Plan::release_refine() {
+  if (!refine) return;
+  if (refine->d_tab) cudaFree(refine->d_tab);
+  if (refine->d_status) cudaFree(refine->d_status);
+  delete refine;
+  refine = nullptr;
+}
+
+int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsParams& rp, double s,
+                     cudaStream_t stream) {
+  if (!refine || !refine->d_tab) {
+    set_error("plan has no FP32 tables");
+    return NTK_ERR_INVALID;
+  }
+  if (rp.kind != RHS_IDENTITY && rp.kind != RHS_COMPACT) {
+    set_error("FP32/refine supports the identity and compact right-hand sides");
+    return NTK_ERR_UNSUPPORTED;
+  }
+  if (rp.kind == RHS_COMPACT && n < 4) {
+    set_error("compact derivative needs n >= 4");
+    return NTK_ERR_INVALID;
+  }
+  RefineArgs ra;
+  ra.tab = refine->d_tab;
+  ra.ai = to_dw(mat.ai);
+  ra.bi = to_dw(mat.bi);
+  ra.ci = to_dw(mat.ci);
+  ra.nh = mat.nh;
+  ra.nt = mat.nt;
+  for (int i = 0; i < 2; ++i) {
+    ra.ha[i] = mat.ha[i];
+    ra.hb[i] = mat.hb[i];
+    ra.hc[i] = mat.hc[i];
+    ra.ta[i] = mat.ta[i];
+    ra.tb[i] = mat.tb[i];
+    ra.tc[i] = mat.tc[i];
+  }
+  ra.sigma0 = rp.sigma0;
+  ra.sigmaN = rp.sigmaN;
+  ra.s = to_dw(s);
+  ra.unit_scale = (s == 1.0) ? 1 : 0;
+  ra.status = refine->d_status;
+  const int W = 8;
+  const int sweeps_eff = (precision == NTK_FP32) ? 0 : sweeps;
+  switch (refine->M) {
+    case 2: return refine_dispatch<2>(in, out, n, b, ra, refine->pow2, sweeps_eff, rp.kind, W, stream);
+    case 4: return refine_dispatch<4>(in, out, n, b, ra, refine->pow2, sweeps_eff, rp.kind, W, stream);
+    case 8: return refine_dispatch<8>(in, out, n, b, ra, refine->pow2, sweeps_eff, rp.kind, W, stream);
+    case 16: return refine_dispatch<16>(in, out, n, b, ra, refine->pow2, sweeps_eff, rp.kind, W, stream);
+    default: return refine_dispatch<32>(in, out, n, b, ra, refine->pow2, sweeps_eff, rp.kind, W, stream);
+  }
+}
+
+}  // namespace ntk

@@ -1,0 +1,505 @@
+// ntk_refine.cuh -- FP32 chunked solve + double-word iterative refinement.
+//
+// Replaces the same reference path as ntk_solve_f64.cu (the cyclic
+// reduction of neato.py:8-124, with compact/rhs.py:9-37 fused in) for the
+// precisions NTK_FP32 and NTK_FP32_REFINE.
+//
+// Why this shape on GB300.  HBM delivers ~6.7 TB/s = ~420 G rows/s at 16 B
+// per row, ~1.45 rows per clock per SM.  The FP64 pipe retires ~1.7
+// instructions per clock per SM, so the plain FP64 solve (4 FP64
+// instructions per row) tops out near 30% of HBM.  Here the FP64 pipe is used
+// once per row (the DADD that assembles the FP64 output) and everything else
+// runs on the FP32/INT pipes:
+//   * the FP64 input is split into a float pair with integer operations;
+//   * the RHS difference, the residual r = d - A x and the accumulation of the
+//     correction use error-free transformations (TwoSum/TwoProd), so they
+//     carry ~48 significant bits -- what an FP64 residual would supply for a
+//     1e-12 result (the FP32 solve leaves ~5e-7, one sweep ~(5e-7)^2 * cond);
+//   * the FP32 solves run on register-resident chunks.
+//
+// Work decomposition.  A CTA stages W systems into shared memory with
+// coalesced loads (contiguous systems: lanes walk rows; strided y/z systems:
+// lanes walk adjacent systems, so no permute pass is needed).  One warp
+// solves one system, lane j owning rows [j*M, (j+1)*M).  The solve applies
+// the shared matrix's LU factors (FP64 on the host, rounded to FP32)
+// chunk-wise: each lane runs the forward and backward recurrences over its
+// chunk from zero and the chunk-to-chunk carries of both first-order linear
+// recurrences are resolved with 5-step warp-shuffle scans.  The staged tile
+// uses a padded layout (chunk pitch M+1, system pitch 32(M+1)+1 words), so
+// both the staging accesses and the per-lane chunk accesses are free of bank
+// conflicts; after the RHS is formed, each tile slot holds that row's
+// double-word RHS (two floats) for the residual sweeps.  Rows whose
+// coefficients differ from the interior ones (the matrix's boundary rows and
+// the compact scheme's one-sided boundary stencils) are computed in FP64 by
+// the lane that owns them.
+#pragma once
+#include <cstdio>
+
+#include "ntk_device.cuh"
+#include "ntk_internal.h"
+#include "ntk_plan.h"
+
+namespace ntk {
+
+struct DW {
+  float h, l;
+};
+
+struct RefineArgs {
+  const float* tab = nullptr;  // [3][32][M+1]: l, g = 1/u, w = c/u (padded chunk layout)
+  DW ai, bi, ci;               // interior row coefficients
+  int nh = 1, nt = 1;          // special rows: head 0..nh-1, tail n-nt..n-1
+  double ha[2] = {0, 0}, hb[2] = {1, 1}, hc[2] = {0, 0};
+  double ta[2] = {0, 0}, tb[2] = {1, 1}, tc[2] = {0, 0};
+  double sigma0 = 1.0, sigmaN = 1.0;  // compact boundary RHS scales
+  DW s;                               // output scale x = s * xi
+  int unit_scale = 1;
+  unsigned* status = nullptr;  // bit 0: input outside the FP32+refine range
+};
+
+template <int M>
+int refine_dispatch(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2,
+                    int sweeps, int rhs, int W, cudaStream_t st);
+
+namespace refine_detail {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+template <int M>
+__host__ __device__ constexpr int sys_pitch() {
+  return 32 * (M + 1) + 1;
+}
+template <int M>
+__device__ __forceinline__ int tile_off(int r) {
+  return (r / M) * (M + 1) + (r % M);
+}
+
+// FP32 chunked LU solve, in place on v (RHS in, solution out); t is scratch.
+template <int M>
+__device__ __forceinline__ void chunk_solve(float (&v)[M], float (&t)[M], const float* tl, const float* tg,
+                                            const float* tw, unsigned lane) {
+  float yh = 0.f, phi = 1.f;
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    const float l = tl[k];
+    yh = fmaf(-l, yh, v[k]);
+    phi = -l * phi;
+    v[k] = yh;
+    t[k] = phi;
+  }
+  float A = phi, B = yh;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const float Ap = __shfl_up_sync(FULL, A, d);
+    const float Bp = __shfl_up_sync(FULL, B, d);
+    if (lane >= (unsigned)d) {
+      B = fmaf(A, Bp, B);
+      A = A * Ap;
+    }
+  }
+  float Yprev = __shfl_up_sync(FULL, B, 1);
+  if (lane == 0) Yprev = 0.f;
+  float xh = 0.f, psi = 1.f;
+#pragma unroll
+  for (int k = M - 1; k >= 0; --k) {
+    const float y = fmaf(t[k], Yprev, v[k]);
+    const float w = tw[k];
+    xh = fmaf(-w, xh, tg[k] * y);
+    psi = -w * psi;
+    v[k] = xh;
+    t[k] = psi;
+  }
+  float A2 = psi, B2 = xh;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const float Ap = __shfl_down_sync(FULL, A2, d);
+    const float Bp = __shfl_down_sync(FULL, B2, d);
+    if (lane + d < 32u) {
+      B2 = fmaf(A2, Bp, B2);
+      A2 = A2 * Ap;
+    }
+  }
+  float Xnext = __shfl_down_sync(FULL, B2, 1);
+  if (lane == 31) Xnext = 0.f;
+#pragma unroll
+  for (int k = 0; k < M; ++k) v[k] = fmaf(t[k], Xnext, v[k]);
+}
+
+// r = D - A*x for one interior row, x = xh (+ xl): the three big products are
+// exact (TwoProd, or exact outright for power-of-two coefficients) and are
+// summed with TwoSum so the cancellation loses nothing; the rounding errors
+// and the xl terms are collected in the tail.
+template <bool POW2, bool HASLO>
+__device__ __forceinline__ float residual_row(float dh, float dl, float xm, float x0, float xp, float lm, float l0,
+                                              float lp, const RefineArgs& a) {
+  float pa, pb, pc, ea = 0.f, eb = 0.f, ec = 0.f;
+  if (POW2) {
+    pa = __fmul_rn(a.ai.h, xm);
+    pb = __fmul_rn(a.bi.h, x0);
+    pc = __fmul_rn(a.ci.h, xp);
+  } else {
+    two_prod(a.ai.h, xm, pa, ea);
+    two_prod(a.bi.h, x0, pb, eb);
+    two_prod(a.ci.h, xp, pc, ec);
+  }
+  float s1, t1, s2, t2, s3, t3;
+  two_sum(dh, -pb, s1, t1);
+  two_sum(s1, -pa, s2, t2);
+  two_sum(s2, -pc, s3, t3);
+  float tail = dl + (t1 + (t2 + t3));
+  if (!POW2) {
+    tail -= (ea + eb) + ec;
+    tail -= fmaf(a.ai.l, xm, fmaf(a.bi.l, x0, a.ci.l * xp));
+  }
+  if (HASLO) tail -= fmaf(a.ai.h, lm, fmaf(a.bi.h, l0, a.ci.h * lp));
+  return s3 + tail;
+}
+
+// FP64 residual of a special row from FP64 neighbours.
+__device__ __forceinline__ float residual_special(double d, double xm, double x0, double xp, double a, double b,
+                                                  double c) {
+  return (float)(d - (a * xm + b * x0 + c * xp));
+}
+
+__device__ __forceinline__ double head_a(const RefineArgs& a, int r) { return r == 0 ? 0.0 : a.ha[r]; }
+
+// D = f_{k+1} - f_{k-1} in double-word
+__device__ __forceinline__ void diff_dw(float ph, float pl, float mh, float ml, float& dh, float& dl) {
+  float s, t;
+  two_sum(ph, -mh, s, t);
+  dh = s;
+  dl = (pl - ml) + t;
+}
+
+template <int M, int RHS, int SWEEPS, bool POW2, bool PAD>
+__global__ void __launch_bounds__(256) refine_kernel(const double* in, double* out, int n, Batch b, RefineArgs ra) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int P = sys_pitch<M>();
+  constexpr int NP = 32 * M;
+  const int W = blockDim.x >> 5;
+  double* tile = reinterpret_cast<double*>(smem_raw);
+  float* tab = reinterpret_cast<float*>(tile + (size_t)W * P);
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const unsigned lane = tid & 31;
+  const long long s0 = (long long)blockIdx.x * W;
+  const int wcount = (int)((b.nsys - s0) < W ? (b.nsys - s0) : W);
+
+  for (int i = tid; i < 3 * 32 * (M + 1); i += blockDim.x) tab[i] = ra.tab[i];
+
+  // ---- stage the W systems (coalesced) ----
+  if (b.es == 1) {
+    for (int w = warp; w < wcount; w += W) {
+      const long long s = s0 + w;
+      const double* src = in + (s / b.ni) * b.os + (s % b.ni) * b.is;
+      double* trow = tile + (size_t)w * P;
+      if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+        for (int r = 2 * lane; r < NP; r += 64) {
+          double2 v = make_double2(0.0, 0.0);
+          if (r + 1 < n) {
+            v = *reinterpret_cast<const double2*>(src + r);
+          } else if (r < n) {
+            v.x = src[r];
+          }
+          trow[tile_off<M>(r)] = v.x;
+          trow[tile_off<M>(r + 1)] = v.y;
+        }
+      } else {
+        for (int r = lane; r < NP; r += 32) trow[tile_off<M>(r)] = (r < n) ? src[r] : 0.0;
+      }
+    }
+  } else {
+    // thread -> fixed system w = tid % W and every (blockDim / W)-th row: a
+    // warp reads 32 / W rows of W adjacent systems per instruction
+    const int w = tid % W;
+    const int rstep = blockDim.x / W;
+    if (w < wcount) {
+      const long long s = s0 + w;
+      const double* src = in + (s / b.ni) * b.os + (s % b.ni) * b.is;
+      double* trow = tile + (size_t)w * P;
+      for (int r = tid / W; r < NP; r += rstep) trow[tile_off<M>(r)] = (r < n) ? src[(long long)r * b.es] : 0.0;
+    }
+  }
+  __syncthreads();
+
+  if (warp < wcount) {
+    double* trow = tile + (size_t)warp * P;
+    const int j = lane;
+    const int r0 = j * M;
+    const int cb = j * (M + 1);  // this lane's chunk in the tile
+    float2* drow = reinterpret_cast<float2*>(trow);
+    const float* tl = tab + 0 * 32 * (M + 1) + cb;
+    const float* tg = tab + 1 * 32 * (M + 1) + cb;
+    const float* tw = tab + 2 * 32 * (M + 1) + cb;
+    const int n1 = n - 1;
+    const bool tail_here = (r0 <= n1) && (n1 < r0 + M);  // owns row n-1
+    unsigned range = 0;
+    float x[M];
+
+    // ---- RHS in double-word, written back into the tile slots ----
+    if (RHS == RHS_COMPACT) {
+      double dsp0 = 0.0, dsp1 = 0.0;  // one-sided boundary stencils (compact/rhs.py:21-31), FP64
+      if (j == 0) dsp0 = ra.sigma0 * ((-5.0 * trow[tile_off<M>(0)] + 4.0 * trow[tile_off<M>(1)]) + trow[tile_off<M>(2)]);
+      if (tail_here)
+        dsp1 = ra.sigmaN * ((-5.0 * trow[tile_off<M>(n1)] + 4.0 * trow[tile_off<M>(n1 - 1)]) + trow[tile_off<M>(n1 - 2)]);
+      __syncwarp();
+      float c0h, c0l, c1h, c1l;  // f_0 and f_1 of the chunk
+      split_f64(trow[cb + 0], c0h, c0l, range);
+      split_f64(trow[cb + 1], c1h, c1l, range);
+      float mh = c0h, ml = c0l, zh = c1h, zl = c1l;  // f_{k-2}, f_{k-1}
+#pragma unroll
+      for (int k = 2; k < M; ++k) {
+        float fh, fl;
+        split_f64(trow[cb + k], fh, fl, range);
+        float dl;
+        diff_dw(fh, fl, mh, ml, x[k - 1], dl);
+        drow[cb + k - 1] = make_float2(x[k - 1], dl);
+        mh = zh;
+        ml = zl;
+        zh = fh;
+        zl = fl;
+      }
+      // edge rows of the chunk need the neighbours' f
+      const float Lh = __shfl_up_sync(FULL, zh, 1), Ll = __shfl_up_sync(FULL, zl, 1);
+      const float Rh = __shfl_down_sync(FULL, c0h, 1), Rl = __shfl_down_sync(FULL, c0l, 1);
+      {
+        float dl;
+        diff_dw(c1h, c1l, Lh, Ll, x[0], dl);
+        drow[cb + 0] = make_float2(x[0], dl);
+        diff_dw(Rh, Rl, (M >= 2 ? mh : Lh), (M >= 2 ? ml : Ll), x[M - 1], dl);
+        drow[cb + M - 1] = make_float2(x[M - 1], dl);
+      }
+      if (j == 0) {
+        float h, l;
+        split_f64(dsp0, h, l, range);
+        x[0] = h;
+        drow[cb + 0] = make_float2(h, l);
+      }
+      if (tail_here) {
+        float h, l;
+        split_f64(dsp1, h, l, range);
+        if (!PAD) {
+          x[M - 1] = h;
+        } else {
+#pragma unroll
+          for (int k = 0; k < M; ++k)
+            if (r0 + k == n1) x[k] = h;
+        }
+        drow[tile_off<M>(n1)] = make_float2(h, l);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < M; ++k) {
+        float h, l;
+        split_f64(trow[cb + k], h, l, range);
+        x[k] = h;
+        drow[cb + k] = make_float2(h, l);
+      }
+    }
+
+    // ---- FP32 solve ----
+    float tmp[M];
+    chunk_solve<M>(x, tmp, tl, tg, tw, lane);
+
+    // ---- refinement sweeps ----
+    float xl[M];
+#pragma unroll
+    for (int k = 0; k < M; ++k) xl[k] = 0.f;
+#pragma unroll
+    for (int sweep = 0; sweep < SWEEPS; ++sweep) {
+      // every lane executes every shuffle (full mask); edges are zeroed after
+      float xleft = __shfl_up_sync(FULL, x[M - 1], 1);
+      float xright = __shfl_down_sync(FULL, x[0], 1);
+      if (j == 0) xleft = 0.f;
+      if (j == 31) xright = 0.f;
+      float lleft = 0.f, lright = 0.f;
+      if (sweep > 0) {  // sweep is warp-uniform
+        lleft = __shfl_up_sync(FULL, xl[M - 1], 1);
+        lright = __shfl_down_sync(FULL, xl[0], 1);
+        if (j == 0) lleft = 0.f;
+        if (j == 31) lright = 0.f;
+      }
+      float r[M];
+#pragma unroll
+      for (int k = 0; k < M; ++k) {
+        const float2 d = drow[cb + k];
+        const float xm = (k == 0) ? xleft : x[k - (k > 0)];
+        const float xp = (k == M - 1) ? xright : x[k + (k < M - 1)];
+        if (sweep == 0) {
+          r[k] = residual_row<POW2, false>(d.x, d.y, xm, x[k], xp, 0.f, 0.f, 0.f, ra);
+        } else {
+          const float lm = (k == 0) ? lleft : xl[k - (k > 0)];
+          const float lp = (k == M - 1) ? lright : xl[k + (k < M - 1)];
+          r[k] = residual_row<POW2, true>(d.x, d.y, xm, x[k], xp, lm, xl[k], lp, ra);
+        }
+      }
+      // head rows (lane 0, compile-time positions), FP64
+      if (j == 0) {
+#pragma unroll
+        for (int k = 0; k < 2 && k < M; ++k) {
+          if (k < ra.nh) {
+            const float2 d = drow[cb + k];
+            const double xm = (k == 0) ? 0.0 : dw_to_f64(x[k - (k > 0)], xl[k - (k > 0)]);
+            const double xp = (k == M - 1) ? dw_to_f64(xright, lright) : dw_to_f64(x[k + (k < M - 1)], xl[k + (k < M - 1)]);
+            r[k] = residual_special((double)d.x + (double)d.y, xm, dw_to_f64(x[k], xl[k]), xp, head_a(ra, k),
+                                    ra.hb[k], ra.hc[k]);
+          }
+        }
+      }
+      // tail rows, FP64
+      if (r0 + M > n - ra.nt && r0 < n) {
+        if (!PAD) {
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            const int k = M - 1 - q;  // row n-1-q
+            if (q < ra.nt && k >= 0) {
+              const int ti = ra.nt - 1 - q;
+              const float2 d = drow[cb + k];
+              const double xm = (k == 0) ? dw_to_f64(xleft, lleft) : dw_to_f64(x[k - (k > 0)], xl[k - (k > 0)]);
+              const double xp = (q == 0) ? 0.0 : dw_to_f64(x[k + (k < M - 1)], xl[k + (k < M - 1)]);
+              r[k] = residual_special((double)d.x + (double)d.y, xm, dw_to_f64(x[k], xl[k]), xp, ra.ta[ti],
+                                      ra.tb[ti], (q == 0) ? 0.0 : ra.tc[ti]);
+            }
+          }
+        } else {
+          // runtime position: gather the needed values with selects
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            const int row = n1 - q;
+            if (q < ra.nt && row >= r0 && row < r0 + M) {
+              const int kk = row - r0;
+              float xh0 = 0.f, xl0 = 0.f, xhm = 0.f, xlm = 0.f, xhp = 0.f, xlp = 0.f;
+#pragma unroll
+              for (int k = 0; k < M; ++k) {
+                if (k == kk) {
+                  xh0 = x[k];
+                  xl0 = xl[k];
+                }
+                if (k == kk - 1) {
+                  xhm = x[k];
+                  xlm = xl[k];
+                }
+                if (k == kk + 1) {
+                  xhp = x[k];
+                  xlp = xl[k];
+                }
+              }
+              if (kk == 0) {
+                xhm = xleft;
+                xlm = lleft;
+              }
+              if (kk == M - 1) {
+                xhp = xright;
+                xlp = lright;
+              }
+              const int ti = ra.nt - 1 - q;
+              const float2 d = drow[tile_off<M>(row)];
+              const float rr = residual_special((double)d.x + (double)d.y, dw_to_f64(xhm, xlm), dw_to_f64(xh0, xl0),
+                                                q == 0 ? 0.0 : dw_to_f64(xhp, xlp), ra.ta[ti], ra.tb[ti],
+                                                q == 0 ? 0.0 : ra.tc[ti]);
+#pragma unroll
+              for (int k = 0; k < M; ++k)
+                if (k == kk) r[k] = rr;
+            }
+          }
+        }
+      }
+      chunk_solve<M>(r, tmp, tl, tg, tw, lane);
+#pragma unroll
+      for (int k = 0; k < M; ++k) {
+        float h, e;
+        two_sum(x[k], r[k], h, e);
+        e += xl[k];
+        fast_two_sum(h, e, x[k], xl[k]);
+      }
+    }
+
+    // ---- FP64 output: x = s * xi ----
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      float oh = x[k], ol = xl[k];
+      if (!ra.unit_scale) {
+        float p, e;
+        two_prod(ra.s.h, oh, p, e);
+        e = fmaf(ra.s.h, ol, e);
+        e = fmaf(ra.s.l, oh, e);
+        fast_two_sum(p, e, oh, ol);
+      }
+      trow[cb + k] = dw_to_f64(oh, ol);
+    }
+    if (range && ra.status) atomicOr(ra.status, 1u);
+  }
+  __syncthreads();
+
+  // ---- store ----
+  if (b.es == 1) {
+    for (int w = warp; w < wcount; w += W) {
+      const long long s = s0 + w;
+      double* dst = out + (s / b.ni) * b.os + (s % b.ni) * b.is;
+      const double* trow = tile + (size_t)w * P;
+      if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+        for (int r = 2 * lane; r < n; r += 64) {
+          if (r + 1 < n)
+            *reinterpret_cast<double2*>(dst + r) = make_double2(trow[tile_off<M>(r)], trow[tile_off<M>(r + 1)]);
+          else
+            dst[r] = trow[tile_off<M>(r)];
+        }
+      } else {
+        for (int r = lane; r < n; r += 32) dst[r] = trow[tile_off<M>(r)];
+      }
+    }
+  } else {
+    const int w = tid % W;
+    const int rstep = blockDim.x / W;
+    if (w < wcount) {
+      const long long s = s0 + w;
+      double* dst = out + (s / b.ni) * b.os + (s % b.ni) * b.is;
+      const double* trow = tile + (size_t)w * P;
+      for (int r = tid / W; r < n; r += rstep) dst[(long long)r * b.es] = trow[tile_off<M>(r)];
+    }
+  }
+}
+
+template <int M, int RHS, int SWEEPS, bool POW2, bool PAD>
+int launch_one(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, int W, cudaStream_t st) {
+  const size_t smem = (size_t)W * sys_pitch<M>() * sizeof(double) + 3 * 32 * (M + 1) * sizeof(float);
+  auto kern = refine_kernel<M, RHS, SWEEPS, POW2, PAD>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(refine_kernel)");
+  const long long blocks = (b.nsys + W - 1) / W;
+  kern<<<(unsigned)blocks, W * 32, smem, st>>>(in, out, n, b, ra);
+  return cuda_status(cudaGetLastError(), "refine_kernel");
+}
+
+template <int M, int RHS, int SWEEPS>
+int dispatch_pp(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2, int W,
+                cudaStream_t st) {
+  const bool pad = (n != 32 * M);
+  if (pow2)
+    return pad ? launch_one<M, RHS, SWEEPS, true, true>(in, out, n, b, ra, W, st)
+               : launch_one<M, RHS, SWEEPS, true, false>(in, out, n, b, ra, W, st);
+  return pad ? launch_one<M, RHS, SWEEPS, false, true>(in, out, n, b, ra, W, st)
+             : launch_one<M, RHS, SWEEPS, false, false>(in, out, n, b, ra, W, st);
+}
+
+template <int M, int RHS>
+int dispatch_sweeps(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2,
+                    int sweeps, int W, cudaStream_t st) {
+  switch (sweeps) {
+    case 0: return dispatch_pp<M, RHS, 0>(in, out, n, b, ra, pow2, W, st);
+    case 1: return dispatch_pp<M, RHS, 1>(in, out, n, b, ra, pow2, W, st);
+    default: return dispatch_pp<M, RHS, 2>(in, out, n, b, ra, pow2, W, st);
+  }
+}
+
+}  // namespace refine_detail
+
+template <int M>
+int refine_dispatch(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2,
+                    int sweeps, int rhs, int W, cudaStream_t st) {
+  using namespace refine_detail;
+  if (rhs == RHS_COMPACT) return dispatch_sweeps<M, RHS_COMPACT>(in, out, n, b, ra, pow2, sweeps, W, st);
+  return dispatch_sweeps<M, RHS_IDENTITY>(in, out, n, b, ra, pow2, sweeps, W, st);
+}
+
+}  // namespace ntk

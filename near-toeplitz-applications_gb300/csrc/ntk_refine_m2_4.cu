@@ -1,0 +1,9 @@
+// ntk_refine_m2_4.cu -- kernel instances of ntk_refine.cuh (split for parallel builds).
+#include "ntk_refine.cuh"
+
+namespace ntk {
+template int refine_dispatch<2>(const double*, double*, int, const Batch&, const RefineArgs&, bool, int, int,
+                                     int, cudaStream_t);
+template int refine_dispatch<4>(const double*, double*, int, const Batch&, const RefineArgs&, bool, int, int,
+                                     int, cudaStream_t);
+}  // namespace ntk

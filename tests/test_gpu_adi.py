@@ -1,0 +1,114 @@
+"""ADI time stepping (experiments/run-adi.py:59-71) on the GPU against the
+oracle: the reference's own pipeline restated on the CPU (stencil + CR +
+transpose, oracle/ntk_oracle.c) and the same pipeline with LAPACK's banded
+solve.  FP64 tolerance 1e-13 relative, or the reference CR's own distance
+from the banded solve where that is larger (ADI coefficients put identity
+boundary rows next to rows scaled by 1/dx^2, which costs the reference's
+cyclic reduction a few digits)."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-13
+
+
+def _run_gpu(cuda, u, d_x, d_y, dx, dt, steps, graph):
+    import ntk
+
+    tu, tx, ty = [torch.from_numpy(np.ascontiguousarray(a)).to(cuda) for a in (u, d_x, d_y)]
+    with ntk.Adi(u.shape[0], dx, dt) as adi:
+        if graph:
+            adi.run(tu, tx, ty, steps, graph=True)
+        else:
+            for _ in range(steps):
+                adi.step(tu, tx, ty)
+        torch.cuda.synchronize()
+        seg = adi.segments
+    return tu.cpu().numpy(), tx.cpu().numpy(), seg
+
+
+def test_golden_three_steps(cuda, oracle, golden):
+    """Three steps from run-adi.py's initial state, N = 32, vs the reference's
+    own kernels (golden vectors)."""
+    u0 = golden["adi_step_u0"]
+    dx, dt = float(golden["adi_step_dx"]), float(golden["adi_step_dt"])
+    u, _, _ = _run_gpu(cuda, u0, u0.copy(), u0.T.copy(), dx, dt, 3, graph=False)
+    ub, xb, yb = u0.copy(), u0.copy(), u0.T.copy()
+    for _ in range(3):
+        oracle.adi_step_banded(ub, xb, yb, dx, dt)
+    ref = golden["adi_step_u3"]
+    # dt = 0.1 with dx = 1/31 (r = 48): the step amplifies rounding, and two
+    # FP64 solvers (the reference CR and LAPACK) already differ by ~2.1e-13;
+    # ours must be no further from LAPACK than 1.5x that spread
+    spread = oracle.rel_err(ref, ub)
+    assert oracle.rel_err(u, ub) <= max(TOL, 1.5 * spread)
+    assert oracle.rel_err(u, ref) <= oracle.rel_err(u, ub) + spread + TOL
+
+
+@pytest.mark.parametrize("N,r,steps", [(64, 0.5, 10), (256, 0.5, 20), (256, 40.0, 5), (512, 0.5, 5)])
+def test_adi_matches_oracle(cuda, oracle, N, r, steps):
+    from ntk.workloads import gaussians_2d
+
+    dx = 1.0 / (N - 1)
+    dt = 2 * r * dx * dx
+    u0 = gaussians_2d(N, seed=N, device="cpu").numpy()
+    for graph in (False, True):
+        u, d_x, seg = _run_gpu(cuda, u0, u0.copy(), u0.T.copy(), dx, dt, steps, graph)
+        ub, xb, yb = u0.copy(), u0.copy(), u0.T.copy()
+        for _ in range(steps):
+            oracle.adi_step_banded(ub, xb, yb, dx, dt)
+        assert oracle.rel_err(u, ub) < TOL, (graph, seg)
+        assert oracle.rel_err(d_x[1:-1], xb[1:-1]) < TOL
+
+
+def test_adi_reference_pipeline(cuda, oracle):
+    """Against the reference pipeline itself (CR restated), N = 128."""
+    from ntk.workloads import gaussians_2d
+
+    N = 128
+    dx = 1.0 / (N - 1)
+    dt = dx * dx
+    u0 = gaussians_2d(N, seed=3, device="cpu").numpy()
+    u, _, _ = _run_gpu(cuda, u0, u0.copy(), u0.T.copy(), dx, dt, 10, graph=True)
+    ur, xr, yr = u0.copy(), u0.copy(), u0.T.copy()
+    ub, xb, yb = u0.copy(), u0.copy(), u0.T.copy()
+    for _ in range(10):
+        oracle.adi_step(ur, xr, yr, dx, dt)
+        oracle.adi_step_banded(ub, xb, yb, dx, dt)
+    assert oracle.rel_err(u, ur) <= max(TOL, oracle.rel_err(ur, ub) + TOL)
+
+
+def test_full_size_segmented(cuda, oracle):
+    """2048^2, r = 0.5 (the 2D ADI heat workload): segmented sweeps are chosen
+    and 4 steps agree with the banded oracle."""
+    from ntk.workloads import gaussians_2d
+
+    N = 2048
+    dx = 1.0 / (N - 1)
+    dt = dx * dx
+    u0 = gaussians_2d(N, seed=0, device="cpu").numpy()
+    u, _, seg = _run_gpu(cuda, u0, u0.copy(), u0.T.copy(), dx, dt, 4, graph=True)
+    assert seg[2] > 1, seg
+    ub, xb, yb = u0.copy(), u0.copy(), u0.T.copy()
+    for _ in range(4):
+        oracle.adi_step_banded(ub, xb, yb, dx, dt)
+    assert oracle.rel_err(u, ub) < TOL
+
+
+def test_graph_replay_is_repeatable(cuda):
+    import ntk
+    from ntk.workloads import gaussians_2d
+
+    N = 256
+    dx = 1.0 / (N - 1)
+    u0 = gaussians_2d(N, seed=1, device=cuda)
+    outs = []
+    with ntk.Adi(N, dx, dx * dx) as adi:
+        for _ in range(2):
+            u, dx_, dy_ = u0.clone(), u0.clone(), u0.t().contiguous()
+            adi.run(u, dx_, dy_, 7, graph=True)
+            torch.cuda.synchronize()
+            outs.append(u.cpu())
+    assert torch.equal(outs[0], outs[1])

@@ -1,0 +1,121 @@
+"""Uneven batches (one persistent launch over systems of different lengths
+and coefficients) against per-system banded solves (SciPy/LAPACK, FP64).
+Tolerance 1e-13 relative per system."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-13
+
+
+def _descriptors(lengths, systems):
+    interior = np.array([s[0] for s in systems])
+    head = np.array([s[1] for s in systems])
+    tail = np.array([s[2] for s in systems])
+    return interior, head, tail
+
+
+def _bands(n, interior, head, tail):
+    a = np.full(n, interior[0])
+    b = np.full(n, interior[1])
+    c = np.full(n, interior[2])
+    for r in range(2):
+        a[r], b[r], c[r] = head[r]
+    for r in range(2):
+        a[n - 2 + r], b[n - 2 + r], c[n - 2 + r] = tail[r]
+    a[0] = 0.0
+    c[-1] = 0.0
+    return a, b, c
+
+
+def _check(cuda, oracle, lengths, interior, head, tail, seed, offsets=None):
+    import ntk
+
+    with ntk.UnevenBatch(lengths, interior, head, tail, offsets=offsets) as bt:
+        total = bt.elements
+        d = np.random.default_rng(seed).normal(size=total)
+        t = torch.from_numpy(d).to(cuda)
+        bt.solve(t)
+        torch.cuda.synchronize()
+        x = t.cpu().numpy()
+        info = bt.info()
+        offs = bt.offsets
+    worst = 0.0
+    for s, n in enumerate(lengths):
+        o = int(offs[s])
+        a, b, c = _bands(int(n), interior[s], head[s], tail[s])
+        ref = oracle.tridiagonal_solve(a, b, c, d[o:o + n])
+        worst = max(worst, oracle.rel_err(x[o:o + n], ref))
+    return worst, info, x, d
+
+
+def test_uneven_workload_4096(cuda, oracle):
+    """4096 systems, lengths log-uniform in [32, 8192], b = 1, a, c ~ U(0.1, 0.3),
+    random diagonally dominant end rows, RHS N(0, 1)."""
+    from ntk.workloads import uneven_batch
+
+    lengths, systems = uneven_batch(4096, seed=0)
+    interior, head, tail = _descriptors(lengths, systems)
+    worst, info, _, _ = _check(cuda, oracle, lengths, interior, head, tail, seed=1)
+    assert worst < TOL
+    assert info["max_n"] <= 8192 and info["segmented"] > 0
+
+
+@pytest.mark.parametrize("n", [3, 4, 5, 31, 130, 1000, 20000])
+def test_single_lengths(cuda, oracle, n):
+    rng = np.random.default_rng(n)
+    k = 5
+    lengths = np.full(k, n)
+    interior = np.column_stack([rng.uniform(0.1, 0.3, k), np.ones(k), rng.uniform(0.1, 0.3, k)])
+    head = rng.uniform(-0.3, 0.3, size=(k, 2, 3))
+    head[:, :, 1] = 2.0
+    tail = rng.uniform(-0.3, 0.3, size=(k, 2, 3))
+    tail[:, :, 1] = 2.0
+    worst, _, _, _ = _check(cuda, oracle, lengths, interior, head, tail, seed=n)
+    assert worst < TOL
+
+
+def test_weak_decay_falls_back_to_one_lane(cuda, oracle):
+    """a = c = 0.49, b = 1: the factors decay too slowly for an exact halo,
+    so the system runs unsegmented and is still exact."""
+    n = 4096
+    lengths = np.array([n, 300])
+    interior = np.array([[0.49, 1.0, 0.49], [0.2, 1.0, 0.2]])
+    head = np.array([[[0, 1.0, 0.49], [0.49, 1.0, 0.49]]] * 2)
+    tail = np.array([[[0.49, 1.0, 0.49], [0.49, 1.0, 0]]] * 2)
+    worst, info, _, _ = _check(cuda, oracle, lengths, interior, head, tail, seed=4)
+    assert worst < 1e-12
+
+
+def test_gapped_offsets_leave_gaps_untouched(cuda, oracle):
+    lengths = np.array([50, 70, 90])
+    offsets = np.array([5, 100, 300])
+    interior = np.tile([0.2, 1.0, 0.25], (3, 1))
+    head = np.tile([[0, 1.5, 0.3], [0.2, 1.2, 0.3]], (3, 1, 1))
+    tail = np.tile([[0.2, 1.1, 0.3], [0.3, 1.4, 0]], (3, 1, 1))
+    worst, _, x, d = _check(cuda, oracle, lengths, interior, head, tail, seed=5, offsets=offsets)
+    assert worst < TOL
+    untouched = np.ones(len(d), bool)
+    for o, n in zip(offsets, lengths):
+        untouched[o:o + n] = False
+    assert np.array_equal(x[untouched], d[untouched])
+
+
+def test_overlap_and_bad_length_rejected(cuda):
+    import ntk
+
+    inter = np.tile([0.2, 1.0, 0.2], (2, 1))
+    hd = np.tile([[0, 1.0, 0.2], [0.2, 1.0, 0.2]], (2, 1, 1))
+    with pytest.raises(ValueError, match="overlap"):
+        ntk.UnevenBatch([10, 10], inter, hd, hd, offsets=[0, 5])
+    with pytest.raises(ValueError):
+        ntk.UnevenBatch([2, 10], inter, hd, hd)
+
+
+def test_empty_batch(cuda):
+    import ntk
+
+    with ntk.UnevenBatch(np.zeros(0, int), np.zeros((0, 3)), np.zeros((0, 2, 3)), np.zeros((0, 2, 3))) as bt:
+        bt.solve(torch.zeros(1, dtype=torch.float64, device=cuda))
