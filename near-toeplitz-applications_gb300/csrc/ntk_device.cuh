@@ -38,26 +38,27 @@ __device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
 // FP64 <-> double-word without the FP64 pipe
 // ---------------------------------------------------------------------------
 // Splits x into hi + lo with hi = x truncated to 24 significant bits and lo
-// the rest rounded to a float (about 48 significant bits in all).  Valid for
-// 2^-126 <= |x| < 2^128; zero maps to (0, 0); smaller magnitudes flush to
-// zero; larger ones (and inf/nan) raise *range_flag.
+// the next 23 bits (47 significant bits in all), using only INT and FP32
+// operations: the double->float conversion and I2F both issue on GB300's slow
+// FP64-rate pipe.  lo is built exactly with the magic-number trick: the 23
+// bits are placed under the exponent of 2^23 and 2^23 is subtracted.
+// Valid for 2^-80 <= |x| < 2^128 (lo is dropped below 2^-80, hi and lo are 0
+// below 2^-126); larger magnitudes, inf and nan raise range_flag.
 __device__ __forceinline__ void split_f64(double x, float& hi, float& lo, unsigned& range_flag) {
   const unsigned h = (unsigned)__double2hiint(x);
   const unsigned l = (unsigned)__double2loint(x);
-  const unsigned sign = h & 0x80000000u;
   const unsigned mag = h & 0x7fffffffu;
-  const unsigned e = mag >> 20;  // biased double exponent
-  // float bits of the truncated value: exponent re-biased by 1023-127=896
-  const unsigned hb = __funnelshift_l(l, mag - (896u << 20), 3);
-  // remaining 29 bits l[28:0] weigh 2^(e-1075); as a float: I2F then scale
-  const float tail = __uint2float_rn(l & 0x1fffffffu);
-  const float scale = __uint_as_float((e - 948u) << 23);  // 2^(e-1075), valid for e >= 949
-  const bool normal = (e >= 897u) & (e <= 1150u);
-  hi = normal ? __uint_as_float(hb | sign) : 0.0f;
-  float t = __fmul_rn(tail, scale);
-  t = (e >= 949u) ? t : 0.0f;
-  lo = normal ? __uint_as_float(__float_as_uint(t) | sign) : 0.0f;
-  range_flag |= (e > 1150u) ? 1u : 0u;
+  // ((h - 896<<20) << 3) | (l >> 29): the sign bit is shifted out
+  const unsigned hb = __funnelshift_l(l, h - (896u << 20), 3);
+  const unsigned sign = h & 0x80000000u;
+  const float hv = __uint_as_float((hb & 0x7fffffffu) | sign);
+  // bits l[28:6] as an exact float integer, weight 2^(e-1069)
+  const float t = __fsub_rn(__uint_as_float(((l >> 6) & 0x007fffffu) | 0x4b000000u), 8388608.0f);
+  const float sc = __uint_as_float((hb & 0x7f800000u) - (46u << 23));
+  const float lv = __uint_as_float(__float_as_uint(__fmul_rn(t, sc)) | sign);
+  hi = (mag >= (897u << 20)) ? hv : 0.0f;
+  lo = (mag >= (943u << 20)) ? lv : 0.0f;
+  range_flag |= (mag >= (1151u << 20)) ? 1u : 0u;
 }
 
 // float -> double by bit manipulation (normal floats and zero; denormals
@@ -79,6 +80,16 @@ __device__ __forceinline__ double dw_to_f64(float hi, float lo) {
   return f32_to_f64_bits(hi) + f32_to_f64_bits(lo);
 #endif
 }
+
+// ---------------------------------------------------------------------------
+// asynchronous global -> shared copies (cp.async, 8 bytes).  src_bytes = 0
+// zero-fills the destination without reading src.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, unsigned src_bytes) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // ---------------------------------------------------------------------------
 // small utilities

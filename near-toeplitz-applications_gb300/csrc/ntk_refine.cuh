@@ -125,10 +125,12 @@ __device__ __forceinline__ void chunk_solve(float (&v)[M], float (&t)[M], const 
   for (int k = 0; k < M; ++k) v[k] = fmaf(t[k], Xnext, v[k]);
 }
 
-// r = D - A*x for one interior row, x = xh (+ xl): the three big products are
-// exact (TwoProd, or exact outright for power-of-two coefficients) and are
-// summed with TwoSum so the cancellation loses nothing; the rounding errors
-// and the xl terms are collected in the tail.
+// r = D - A*x for one interior row, x = xh (+ xl).  A*xh is formed as an
+// exact double-word p + ep: the products are exact (power-of-two
+// coefficients) or split with TwoProd, and are summed with TwoSum.  dh - p is
+// then exact whenever it cancels (Sterbenz: dh and p within a factor of 2),
+// and otherwise its rounding is relative to r itself, so no third TwoSum is
+// needed; the low-order terms are collected in the tail.
 template <bool POW2, bool HASLO>
 __device__ __forceinline__ float residual_row(float dh, float dl, float xm, float x0, float xp, float lm, float l0,
                                               float lp, const RefineArgs& a) {
@@ -142,17 +144,16 @@ __device__ __forceinline__ float residual_row(float dh, float dl, float xm, floa
     two_prod(a.bi.h, x0, pb, eb);
     two_prod(a.ci.h, xp, pc, ec);
   }
-  float s1, t1, s2, t2, s3, t3;
-  two_sum(dh, -pb, s1, t1);
-  two_sum(s1, -pa, s2, t2);
-  two_sum(s2, -pc, s3, t3);
-  float tail = dl + (t1 + (t2 + t3));
+  float s, es, p, ep;
+  two_sum(pa, pc, s, es);
+  two_sum(pb, s, p, ep);
+  float tail = __fsub_rn(dl, __fadd_rn(ep, es));
   if (!POW2) {
     tail -= (ea + eb) + ec;
     tail -= fmaf(a.ai.l, xm, fmaf(a.bi.l, x0, a.ci.l * xp));
   }
   if (HASLO) tail -= fmaf(a.ai.h, lm, fmaf(a.bi.h, l0, a.ci.h * lp));
-  return s3 + tail;
+  return __fadd_rn(__fsub_rn(dh, p), tail);
 }
 
 // FP64 residual of a special row from FP64 neighbours.
@@ -163,16 +164,17 @@ __device__ __forceinline__ float residual_special(double d, double xm, double x0
 
 __device__ __forceinline__ double head_a(const RefineArgs& a, int r) { return r == 0 ? 0.0 : a.ha[r]; }
 
-// D = f_{k+1} - f_{k-1} in double-word
-__device__ __forceinline__ void diff_dw(float ph, float pl, float mh, float ml, float& dh, float& dl) {
-  float s, t;
-  two_sum(ph, -mh, s, t);
-  dh = s;
-  dl = (pl - ml) + t;
-}
+#ifndef NTK_REFINE_OCC
+#define NTK_REFINE_OCC 3
+#endif
+template <int M>
+struct RefineOcc {
+  static constexpr int value = (M <= 16) ? NTK_REFINE_OCC : 1;
+};
 
 template <int M, int RHS, int SWEEPS, bool POW2, bool PAD>
-__global__ void __launch_bounds__(256) refine_kernel(const double* in, double* out, int n, Batch b, RefineArgs ra) {
+__global__ void __launch_bounds__(256, RefineOcc<M>::value)
+    refine_kernel(const double* in, double* out, int n, Batch b, RefineArgs ra) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int P = sys_pitch<M>();
   constexpr int NP = 32 * M;
@@ -187,26 +189,14 @@ __global__ void __launch_bounds__(256) refine_kernel(const double* in, double* o
 
   for (int i = tid; i < 3 * 32 * (M + 1); i += blockDim.x) tab[i] = ra.tab[i];
 
-  // ---- stage the W systems (coalesced) ----
+  // ---- stage the W systems: coalesced cp.async, all copies in flight at once ----
   if (b.es == 1) {
     for (int w = warp; w < wcount; w += W) {
       const long long s = s0 + w;
       const double* src = in + (s / b.ni) * b.os + (s % b.ni) * b.is;
       double* trow = tile + (size_t)w * P;
-      if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
-        for (int r = 2 * lane; r < NP; r += 64) {
-          double2 v = make_double2(0.0, 0.0);
-          if (r + 1 < n) {
-            v = *reinterpret_cast<const double2*>(src + r);
-          } else if (r < n) {
-            v.x = src[r];
-          }
-          trow[tile_off<M>(r)] = v.x;
-          trow[tile_off<M>(r + 1)] = v.y;
-        }
-      } else {
-        for (int r = lane; r < NP; r += 32) trow[tile_off<M>(r)] = (r < n) ? src[r] : 0.0;
-      }
+#pragma unroll 4
+      for (int r = lane; r < NP; r += 32) cp_async8(trow + tile_off<M>(r), src + (r < n ? r : 0), r < n ? 8u : 0u);
     }
   } else {
     // thread -> fixed system w = tid % W and every (blockDim / W)-th row: a
@@ -217,9 +207,12 @@ __global__ void __launch_bounds__(256) refine_kernel(const double* in, double* o
       const long long s = s0 + w;
       const double* src = in + (s / b.ni) * b.os + (s % b.ni) * b.is;
       double* trow = tile + (size_t)w * P;
-      for (int r = tid / W; r < NP; r += rstep) trow[tile_off<M>(r)] = (r < n) ? src[(long long)r * b.es] : 0.0;
+#pragma unroll 4
+      for (int r = tid / W; r < NP; r += rstep)
+        cp_async8(trow + tile_off<M>(r), src + (long long)(r < n ? r : 0) * b.es, r < n ? 8u : 0u);
     }
   }
+  cp_async_wait_all();
   __syncthreads();
 
   if (warp < wcount) {
@@ -238,46 +231,39 @@ __global__ void __launch_bounds__(256) refine_kernel(const double* in, double* o
 
     // ---- RHS in double-word, written back into the tile slots ----
     if (RHS == RHS_COMPACT) {
+      // D_r = f_{r+1} - f_{r-1} is formed in FP64 (one DADD, as in the FP64
+      // path) and then split: a double-word split of f itself keeps only
+      // ~2^-47 |f|, too coarse when f_{r+1} and f_{r-1} nearly cancel.
       double dsp0 = 0.0, dsp1 = 0.0;  // one-sided boundary stencils (compact/rhs.py:21-31), FP64
       if (j == 0) dsp0 = ra.sigma0 * ((-5.0 * trow[tile_off<M>(0)] + 4.0 * trow[tile_off<M>(1)]) + trow[tile_off<M>(2)]);
       if (tail_here)
         dsp1 = ra.sigmaN * ((-5.0 * trow[tile_off<M>(n1)] + 4.0 * trow[tile_off<M>(n1 - 1)]) + trow[tile_off<M>(n1 - 2)]);
-      __syncwarp();
-      float c0h, c0l, c1h, c1l;  // f_0 and f_1 of the chunk
-      split_f64(trow[cb + 0], c0h, c0l, range);
-      split_f64(trow[cb + 1], c1h, c1l, range);
-      float mh = c0h, ml = c0l, zh = c1h, zl = c1l;  // f_{k-2}, f_{k-1}
+      const double fleft = (j > 0) ? trow[tile_off<M>(r0 - 1)] : 0.0;
+      const double fright = (j < 31) ? trow[tile_off<M>(r0 + M)] : 0.0;
+      __syncwarp();  // the neighbours' halo reads happen before any slot is rewritten
+      double fprev = fleft, fcur = trow[cb];
 #pragma unroll
-      for (int k = 2; k < M; ++k) {
-        float fh, fl;
-        split_f64(trow[cb + k], fh, fl, range);
-        float dl;
-        diff_dw(fh, fl, mh, ml, x[k - 1], dl);
-        drow[cb + k - 1] = make_float2(x[k - 1], dl);
-        mh = zh;
-        ml = zl;
-        zh = fh;
-        zl = fl;
-      }
-      // edge rows of the chunk need the neighbours' f
-      const float Lh = __shfl_up_sync(FULL, zh, 1), Ll = __shfl_up_sync(FULL, zl, 1);
-      const float Rh = __shfl_down_sync(FULL, c0h, 1), Rl = __shfl_down_sync(FULL, c0l, 1);
-      {
-        float dl;
-        diff_dw(c1h, c1l, Lh, Ll, x[0], dl);
-        drow[cb + 0] = make_float2(x[0], dl);
-        diff_dw(Rh, Rl, (M >= 2 ? mh : Lh), (M >= 2 ? ml : Ll), x[M - 1], dl);
-        drow[cb + M - 1] = make_float2(x[M - 1], dl);
+      for (int k = 0; k < M; ++k) {
+        const double fnext = (k < M - 1) ? trow[cb + k + 1] : fright;
+        float h, l;
+        split_f64(fnext - fprev, h, l, range);
+        fast_two_sum(h, l, h, l);
+        x[k] = h;
+        drow[cb + k] = make_float2(h, l);
+        fprev = fcur;
+        fcur = fnext;
       }
       if (j == 0) {
         float h, l;
         split_f64(dsp0, h, l, range);
+        fast_two_sum(h, l, h, l);
         x[0] = h;
         drow[cb + 0] = make_float2(h, l);
       }
       if (tail_here) {
         float h, l;
         split_f64(dsp1, h, l, range);
+        fast_two_sum(h, l, h, l);
         if (!PAD) {
           x[M - 1] = h;
         } else {
@@ -292,6 +278,7 @@ __global__ void __launch_bounds__(256) refine_kernel(const double* in, double* o
       for (int k = 0; k < M; ++k) {
         float h, l;
         split_f64(trow[cb + k], h, l, range);
+        fast_two_sum(h, l, h, l);  // h = d rounded to FP32
         x[k] = h;
         drow[cb + k] = make_float2(h, l);
       }
@@ -438,6 +425,7 @@ __global__ void __launch_bounds__(256) refine_kernel(const double* in, double* o
       double* dst = out + (s / b.ni) * b.os + (s % b.ni) * b.is;
       const double* trow = tile + (size_t)w * P;
       if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+#pragma unroll 4
         for (int r = 2 * lane; r < n; r += 64) {
           if (r + 1 < n)
             *reinterpret_cast<double2*>(dst + r) = make_double2(trow[tile_off<M>(r)], trow[tile_off<M>(r + 1)]);
@@ -445,6 +433,7 @@ __global__ void __launch_bounds__(256) refine_kernel(const double* in, double* o
             dst[r] = trow[tile_off<M>(r)];
         }
       } else {
+#pragma unroll 4
         for (int r = lane; r < n; r += 32) dst[r] = trow[tile_off<M>(r)];
       }
     }
@@ -455,6 +444,7 @@ __global__ void __launch_bounds__(256) refine_kernel(const double* in, double* o
       const long long s = s0 + w;
       double* dst = out + (s / b.ni) * b.os + (s % b.ni) * b.is;
       const double* trow = tile + (size_t)w * P;
+#pragma unroll 4
       for (int r = tid / W; r < n; r += rstep) dst[(long long)r * b.es] = trow[tile_off<M>(r)];
     }
   }

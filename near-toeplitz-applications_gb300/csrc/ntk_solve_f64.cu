@@ -299,23 +299,41 @@ __global__ void __launch_bounds__(32) thomas_f64_staged_kernel(const double* __r
   const int pitch = n + 1;
   const long long s0 = (long long)blockIdx.x * 32;
   const int cnt = (int)min(32LL, b.nsys - s0);
-  // stage: one system at a time, lanes walk its rows
+  // stage: one system at a time, lanes walk its rows; cp.async keeps every
+  // copy of the tile in flight at once
   for (int w = 0; w < cnt; ++w) {
     const long long s = s0 + w;
     const double* src = in + (s / b.ni) * b.os + (s % b.ni) * b.is;
     double* trow = tile + w * pitch;
-    for (int r = lane; r < n; r += 32) trow[r] = src[r];
+#pragma unroll 4
+    for (int r = lane; r < n; r += 32) cp_async8(trow + r, src + r, 8u);
   }
+  cp_async_wait_all();
   __syncwarp();
   if (lane < cnt) {
+    // Rows are processed in blocks of 8: the block's loads are issued
+    // together ahead of its dependent FMA chain (the chain, not the loads,
+    // bounds the loop).
+    constexpr int B = 8;
     double* v = tile + lane * pitch;
     double eta;
     if constexpr (RHS == RHS_IDENTITY) {
       eta = v[0];
-#pragma unroll 4
-      for (int i = 1; i < n; ++i) {
-        eta = fma(-__ldg(t.l + i), eta, v[i]);
-        v[i] = eta;
+      for (int i0 = 1; i0 < n; i0 += B) {
+        double fv[B], lv[B];
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+          const int i = min(i0 + k, n - 1);
+          fv[k] = v[i];
+          lv[k] = __ldg(t.l + i);
+        }
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+          if (i0 + k < n) {
+            eta = fma(-lv[k], eta, fv[k]);
+            v[i0 + k] = eta;
+          }
+        }
       }
     } else {
       const double f0 = v[0], f1 = v[1], f2 = v[2];
@@ -323,23 +341,45 @@ __global__ void __launch_bounds__(32) thomas_f64_staged_kernel(const double* __r
       eta = rp.sigma0 * ((-5.0 * f0 + 4.0 * f1) + f2);
       double fm = f0, fc = f1;  // f_{i-1}, f_i
       v[0] = eta;
-#pragma unroll 4
-      for (int i = 1; i < n - 1; ++i) {
-        const double fp = v[i + 1];
-        eta = fma(-__ldg(t.l + i), eta, fp - fm);
-        v[i] = eta;
-        fm = fc;
-        fc = fp;
+      for (int i0 = 1; i0 < n - 1; i0 += B) {
+        double fv[B], lv[B];
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+          const int i = min(i0 + k, n - 2);
+          fv[k] = v[i + 1];
+          lv[k] = __ldg(t.l + i);
+        }
+#pragma unroll
+        for (int k = 0; k < B; ++k) {
+          if (i0 + k < n - 1) {
+            eta = fma(-lv[k], eta, fv[k] - fm);
+            v[i0 + k] = eta;
+            fm = fc;
+            fc = fv[k];
+          }
+        }
       }
       eta = fma(-__ldg(t.l + (n - 1)), eta, rp.sigmaN * ((-5.0 * fl2 + 4.0 * fl1) + fl0));
       v[n - 1] = eta;
     }
     double x = __ldg(t.g + (n - 1)) * eta;
     v[n - 1] = x;
-#pragma unroll 4
-    for (int i = n - 2; i >= 0; --i) {
-      x = fma(-__ldg(t.w + i), x, __ldg(t.g + i) * v[i]);
-      v[i] = x;
+    for (int i0 = n - 2; i0 >= 0; i0 -= B) {
+      double ev[B], gv[B], wv[B];
+#pragma unroll
+      for (int k = 0; k < B; ++k) {
+        const int i = max(i0 - k, 0);
+        ev[k] = v[i];
+        gv[k] = __ldg(t.g + i);
+        wv[k] = __ldg(t.w + i);
+      }
+#pragma unroll
+      for (int k = 0; k < B; ++k) {
+        if (i0 - k >= 0) {
+          x = fma(-wv[k], x, gv[k] * ev[k]);
+          v[i0 - k] = x;
+        }
+      }
     }
   }
   __syncwarp();
@@ -347,6 +387,7 @@ __global__ void __launch_bounds__(32) thomas_f64_staged_kernel(const double* __r
     const long long s = s0 + w;
     double* dst = out + (s / b.ni) * b.os + (s % b.ni) * b.is;
     const double* trow = tile + w * pitch;
+#pragma unroll 4
     for (int r = lane; r < n; r += 32) dst[r] = trow[r];
   }
 }

@@ -34,16 +34,20 @@ def _newest(paths):
     return max((os.path.getmtime(p) for p in paths if os.path.exists(p)), default=0.0)
 
 
-def build(verbose=False, extra_flags=()):
+def build(verbose=False, extra_flags=(), out=None, build_dir=None):
+    """Compile stale objects and link libntk.so.  out/build_dir/extra_flags
+    build a variant elsewhere (used for tuning experiments)."""
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         raise RuntimeError("nvcc not found; libntk.so cannot be built")
-    os.makedirs(BUILD, exist_ok=True)
+    lib_path = out or LIB
+    bdir = build_dir or BUILD
+    os.makedirs(bdir, exist_ok=True)
     hdr_time = max(_newest(_headers()), os.path.getmtime(__file__))
     jobs = []
     objs = []
     for src in _sources():
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(bdir, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), hdr_time):
             jobs.append((src, obj))
@@ -62,14 +66,14 @@ def build(verbose=False, extra_flags=()):
     if jobs:
         with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
             logs = list(ex.map(compile_one, jobs))
-    if jobs or not os.path.exists(LIB) or os.path.getmtime(LIB) < _newest(objs):
-        cmd = [nvcc, ARCH, "-shared", "-o", LIB] + objs + ["-lcudart"]
+    if jobs or not os.path.exists(lib_path) or os.path.getmtime(lib_path) < _newest(objs):
+        cmd = [nvcc, ARCH, "-shared", "-o", lib_path] + objs + ["-lcudart"]
         res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         if res.returncode != 0:
             raise RuntimeError("link failed:\n%s" % res.stdout)
     if verbose:
-        return LIB, "\n".join(logs)
-    return LIB
+        return lib_path, "\n".join(logs)
+    return lib_path
 
 
 if __name__ == "__main__":

@@ -17,6 +17,8 @@
  *                                            block per system, n/2 threads)
  *   ntko_thomas           experiments/run-compact.py:14-28 restated as the
  *                         textbook Thomas algorithm (general tridiagonal)
+ *   ntko_thomas_ld        the same in long double, many right-hand sides: the
+ *                         accuracy reference for badly scaled matrices
  *   ntko_compact_rhs      compact/rhs.py:9-37 (computeRHS)
  *   ntko_permute          compact/permute.py:7-20,32-52 (permuteKernel)
  *   ntko_adi_rhs          adi/rhs.py:10-25,35-55 (applyVerticalStencil)
@@ -179,6 +181,41 @@ int ntko_thomas(int n, const double* a, const double* b, const double* c, const 
   x[n - 1] = dp[n - 1];
   for (int i = n - 2; i >= 0; --i) x[i] = dp[i] - cp[i] * x[i + 1];
   free(cp);
+  free(dp);
+  return 0;
+}
+
+/* The same Thomas algorithm in long double (80-bit x87 on x86-64, IEEE quad
+ * on AArch64) for nrhs right-hand sides stored one after another: the
+ * accuracy reference for badly scaled matrices (the ADI tuples), where
+ * LAPACK's pivoting banded solve and FP64 cyclic reduction both lose digits.
+ * d and x hold nrhs * n values; x may alias d. */
+int ntko_thomas_ld(int n, long nrhs, const double* a, const double* b, const double* c, const double* d, double* x) {
+  if (n < 1 || nrhs < 0) return -1;
+  long double* cp = (long double*)malloc(sizeof(long double) * (size_t)n);
+  long double* den = (long double*)malloc(sizeof(long double) * (size_t)n);
+  long double* dp = (long double*)malloc(sizeof(long double) * (size_t)n);
+  if (!cp || !den || !dp) { free(cp); free(den); free(dp); return -2; }
+  den[0] = (long double)b[0];
+  cp[0] = (n > 1 ? (long double)c[0] : 0.0L) / den[0];
+  for (int i = 1; i < n; ++i) {
+    den[i] = (long double)b[i] - (long double)a[i] * cp[i - 1];
+    cp[i] = (i < n - 1 ? (long double)c[i] : 0.0L) / den[i];
+  }
+  for (long s = 0; s < nrhs; ++s) {
+    const double* ds = d + (size_t)s * n;
+    double* xs = x + (size_t)s * n;
+    dp[0] = (long double)ds[0] / den[0];
+    for (int i = 1; i < n; ++i) dp[i] = ((long double)ds[i] - (long double)a[i] * dp[i - 1]) / den[i];
+    long double xv = dp[n - 1];
+    xs[n - 1] = (double)xv;
+    for (int i = n - 2; i >= 0; --i) {
+      xv = dp[i] - cp[i] * xv;
+      xs[i] = (double)xv;
+    }
+  }
+  free(cp);
+  free(den);
   free(dp);
   return 0;
 }

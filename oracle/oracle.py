@@ -13,7 +13,9 @@ and restates the reference's CPU path with NumPy/SciPy:
 
   tridiagonal_solve      experiments/run-compact.py:14-28 (solve_banded)
   banded_compact_deriv   RHS of compact/rhs.py:21-36 + the banded solve, any axis
-  adi_step_numpy         experiments/run-adi.py:59-71 with the banded solve
+  adi_step_banded        experiments/run-adi.py:59-71 with the banded solve
+  thomas_ld / exact_solve / adi_step_exact   the same in long double: the
+                         accuracy reference for badly scaled (ADI) matrices
 """
 import ctypes
 import os
@@ -50,6 +52,8 @@ def lib():
         L.ntko_cr_solve.argtypes = [ctypes.c_int, ctypes.c_long, _c_double_p, _c_double_p]
         L.ntko_thomas.restype = ctypes.c_int
         L.ntko_thomas.argtypes = [ctypes.c_int] + [_c_double_p] * 5
+        L.ntko_thomas_ld.restype = ctypes.c_int
+        L.ntko_thomas_ld.argtypes = [ctypes.c_int, ctypes.c_long] + [_c_double_p] * 5
         L.ntko_compact_rhs.restype = None
         L.ntko_compact_rhs.argtypes = [_c_double_p, _c_double_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_double]
@@ -156,6 +160,23 @@ def thomas(a, b, c, d):
     if rc:
         raise ValueError("bad system")
     return x
+
+
+def thomas_ld(a, b, c, d):
+    """Thomas in long double for the rows of d (..., n); returns float64."""
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    n = d.shape[-1]
+    out = np.empty_like(d)
+    vecs = [np.ascontiguousarray(v, dtype=np.float64) for v in (a, b, c)]
+    if lib().ntko_thomas_ld(n, d.size // n, *[_ptr(v) for v in vecs], _ptr(d), _ptr(out)):
+        raise ValueError("bad system")
+    return out
+
+
+def exact_solve(d, n, coeffs):
+    """High-precision solve of NearToeplitzSolver's systems (rows of d)."""
+    a, b, c = near_toeplitz_bands(n, coeffs)
+    return thomas_ld(a, b, c, np.asarray(d).reshape(-1, n)).reshape(np.shape(d))
 
 
 def compact_rhs(f, dx):
@@ -267,6 +288,19 @@ def adi_step_banded(u, d_x, d_y, dx, dt):
     for d in (d_x, d_y):
         d[1:-1, 1:-1] = bottom * u[:-2, 1:-1] + center * u[1:-1, 1:-1] + top * u[2:, 1:-1]
         d[1:-1, :] = tridiagonal_solve(a, b, c, d[1:-1, :].T).T
+        u[:, :] = d.T
+
+
+def adi_step_exact(u, d_x, d_y, dx, dt):
+    """experiments/run-adi.py:59-71 with the long-double Thomas solve."""
+    N = u.shape[0]
+    bottom = -1. / (dx * dx)
+    top = -1. / (dx * dx)
+    center = 2 * (-1. / dt + 1. / (dx * dx))
+    a, b, c = near_toeplitz_bands(N, adi_coeffs(dx, dt))
+    for d in (d_x, d_y):
+        d[1:-1, 1:-1] = bottom * u[:-2, 1:-1] + center * u[1:-1, 1:-1] + top * u[2:, 1:-1]
+        d[1:-1, :] = thomas_ld(a, b, c, d[1:-1, :])
         u[:, :] = d.T
 
 
