@@ -58,6 +58,19 @@ int ntk_last_error(char* buf, int len);
 int ntk_plan_create(ntk_plan** out, int n, long long nrhs, const double coeffs[7], int precision,
                     int refine_sweeps);
 
+/* Launch configuration of a plan (what the reference fixes in its jinja2
+ * templates, neato.py:160-163): set by the autotuner (ntk/autotune.py) or by
+ * hand.  Keys and values:
+ *   NTK_TUNE_F64_X_VARIANT  contiguous FP64 sweeps: 0 transposing tile ring
+ *                           (default), 1 whole-system shared tile, 2 direct
+ *   NTK_TUNE_F64_THREADS    threads per block of the one-thread-per-system
+ *                           FP64 kernel: 32, 64, 128 (default)
+ *   NTK_TUNE_REFINE_W       systems (warps) per CTA of the FP32+refine
+ *                           kernel: 4 or 8 (default) */
+enum ntk_tune_key { NTK_TUNE_F64_X_VARIANT = 1, NTK_TUNE_F64_THREADS = 2, NTK_TUNE_REFINE_W = 3 };
+int ntk_plan_set_tuning(ntk_plan* plan, int key, int value);
+int ntk_plan_get_tuning(const ntk_plan* plan, int key, int* value);
+
 /* Frees the plan's device tables.  Synchronous; NULL is accepted. */
 int ntk_plan_destroy(ntk_plan* plan);
 

@@ -137,7 +137,7 @@ int Plan::run(const double* in, double* out, const Batch& b, RhsParams rp, doubl
     t.w = d_lw + n;
     rc = g_table(s, &t.g);
     if (rc) return rc;
-    return launch_thomas_f64(in, out, n, b, rp, t, 128, stream);
+    return launch_thomas_f64(in, out, n, b, rp, t, tune_f64_threads, stream, tune_f64_x_variant);
   }
   return run_refine(in, out, b, rp, s, stream);
 }
@@ -207,6 +207,47 @@ int ntk_plan_create(ntk_plan** out, int n, long long nrhs, const double coeffs[7
   }
   *out = p;
   return NTK_OK;
+}
+
+int ntk_plan_set_tuning(ntk_plan* plan, int key, int value) {
+  if (!plan) {
+    ntk::set_error("ntk_plan_set_tuning: null plan");
+    return NTK_ERR_INVALID;
+  }
+  switch (key) {
+    case NTK_TUNE_F64_X_VARIANT:
+      if (value < 0 || value > 2) break;
+      plan->tune_f64_x_variant = value;
+      return NTK_OK;
+    case NTK_TUNE_F64_THREADS:
+      if (value != 32 && value != 64 && value != 128) break;
+      plan->tune_f64_threads = value;
+      return NTK_OK;
+    case NTK_TUNE_REFINE_W:
+      if (value != 4 && value != 8) break;
+      plan->tune_refine_w = value;
+      return NTK_OK;
+    default:
+      ntk::set_error("ntk_plan_set_tuning: unknown key %d", key);
+      return NTK_ERR_INVALID;
+  }
+  ntk::set_error("ntk_plan_set_tuning: value %d out of range for key %d", value, key);
+  return NTK_ERR_INVALID;
+}
+
+int ntk_plan_get_tuning(const ntk_plan* plan, int key, int* value) {
+  if (!plan || !value) {
+    ntk::set_error("ntk_plan_get_tuning: null argument");
+    return NTK_ERR_INVALID;
+  }
+  switch (key) {
+    case NTK_TUNE_F64_X_VARIANT: *value = plan->tune_f64_x_variant; return NTK_OK;
+    case NTK_TUNE_F64_THREADS: *value = plan->tune_f64_threads; return NTK_OK;
+    case NTK_TUNE_REFINE_W: *value = plan->tune_refine_w; return NTK_OK;
+    default:
+      ntk::set_error("ntk_plan_get_tuning: unknown key %d", key);
+      return NTK_ERR_INVALID;
+  }
 }
 
 int ntk_plan_destroy(ntk_plan* plan) {

@@ -67,8 +67,10 @@ void set_error(const char* fmt, ...);
 int cuda_status(cudaError_t e, const char* where);
 
 // kernels (ntk_solve_f64.cu)
+// x_variant (contiguous systems): 0 = automatic (transposing tile ring),
+// 1 = whole-system shared-memory tile, 2 = direct loads
 int launch_thomas_f64(const double* in, double* out, int n, const Batch& b, const RhsParams& rp,
-                      const TablesF64& t, int threads, cudaStream_t stream);
+                      const TablesF64& t, int threads, cudaStream_t stream, int x_variant = 0);
 int launch_thomas_f64_segmented(const double* in, double* eta, double* out, int n, const Batch& b,
                                 const RhsParams& rp, const TablesF64& t, const SegParams& sp, cudaStream_t stream);
 

@@ -14,6 +14,7 @@ struct RefineState {
   float* d_tab = nullptr;
   unsigned* d_status = nullptr;
   bool pow2 = false;
+  bool decay = false;  // chunk factor products below 2^-26: one-shuffle carries
 };
 
 namespace {
@@ -42,7 +43,7 @@ int Plan::init_refine() {
   }
   refine = st;
   int M = 0;
-  for (int m : {2, 4, 8, 16, 32})
+  for (int m : {4, 8, 16, 32})
     if (n <= 32 * m) {
       M = m;
       break;
@@ -81,6 +82,22 @@ int Plan::init_refine() {
     p2 = p2 && is_pow2_or_zero(mat.a(i)) && is_pow2_or_zero(mat.b(i)) && is_pow2_or_zero(mat.c(i));
   }
   st->pow2 = p2;
+  // carry truncation is exact to FP32 rounding when every chunk's factor
+  // products (over its M rows) are below 2^-26 (only offered for M >= 16)
+  bool dec = (M >= 16);
+  const double lim = std::ldexp(1.0, -26);
+  for (int j = 0; j < 32 && dec; ++j) {
+    double pl = 1.0, pw = 1.0;
+    for (int k = 0; k < M; ++k) {
+      const int r = j * M + k;
+      const double l = r < n ? std::fabs(lu_l[r]) : 0.0;
+      const double w = r < n ? std::fabs((r < n - 1 ? mat.c(r) : 0.0) / lu_u[r]) : 0.0;
+      pl *= l;
+      pw *= w;
+    }
+    dec = (pl <= lim) && (pw <= lim);
+  }
+  st->decay = dec;
   return NTK_OK;
 }
 
@@ -113,27 +130,34 @@ int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsPar
   ra.ci = to_dw(mat.ci);
   ra.nh = mat.nh;
   ra.nt = mat.nt;
+  // special rows as double-word coefficients; row 0 has no a, row n-1 no c
   for (int i = 0; i < 2; ++i) {
-    ra.ha[i] = mat.ha[i];
-    ra.hb[i] = mat.hb[i];
-    ra.hc[i] = mat.hc[i];
-    ra.ta[i] = mat.ta[i];
-    ra.tb[i] = mat.tb[i];
-    ra.tc[i] = mat.tc[i];
+    const int hr = i, tr = n - mat.nt + i;
+    ra.hd[i][0] = to_dw(hr == 0 ? 0.0 : mat.a(hr));
+    ra.hd[i][1] = to_dw(mat.b(hr));
+    ra.hd[i][2] = to_dw(mat.c(hr));
+    ra.td[i][0] = to_dw(tr >= 0 && tr < n ? mat.a(tr) : 0.0);
+    ra.td[i][1] = to_dw(tr >= 0 && tr < n ? mat.b(tr) : 1.0);
+    ra.td[i][2] = to_dw(tr >= 0 && tr < n - 1 ? mat.c(tr) : 0.0);
   }
   ra.sigma0 = rp.sigma0;
   ra.sigmaN = rp.sigmaN;
   ra.s = to_dw(s);
   ra.unit_scale = (s == 1.0) ? 1 : 0;
   ra.status = refine->d_status;
-  const int W = 8;
+  const int W = tune_refine_w;
   const int sweeps_eff = (precision == NTK_FP32) ? 0 : sweeps;
+  const bool d = refine->decay;
+  const bool p2 = refine->pow2;
   switch (refine->M) {
-    case 2: return refine_dispatch<2>(in, out, n, b, ra, refine->pow2, sweeps_eff, rp.kind, W, stream);
-    case 4: return refine_dispatch<4>(in, out, n, b, ra, refine->pow2, sweeps_eff, rp.kind, W, stream);
-    case 8: return refine_dispatch<8>(in, out, n, b, ra, refine->pow2, sweeps_eff, rp.kind, W, stream);
-    case 16: return refine_dispatch<16>(in, out, n, b, ra, refine->pow2, sweeps_eff, rp.kind, W, stream);
-    default: return refine_dispatch<32>(in, out, n, b, ra, refine->pow2, sweeps_eff, rp.kind, W, stream);
+    case 4: return refine_dispatch<4, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+    case 8: return refine_dispatch<8, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+    case 16:
+      return d ? refine_dispatch<16, true>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream)
+               : refine_dispatch<16, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+    default:
+      return d ? refine_dispatch<32, true>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream)
+               : refine_dispatch<32, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
   }
 }
 

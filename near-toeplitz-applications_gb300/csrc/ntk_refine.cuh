@@ -49,15 +49,15 @@ struct RefineArgs {
   const float* tab = nullptr;  // [3][32][M+1]: l, g = 1/u, w = c/u (padded chunk layout)
   DW ai, bi, ci;               // interior row coefficients
   int nh = 1, nt = 1;          // special rows: head 0..nh-1, tail n-nt..n-1
-  double ha[2] = {0, 0}, hb[2] = {1, 1}, hc[2] = {0, 0};
-  double ta[2] = {0, 0}, tb[2] = {1, 1}, tc[2] = {0, 0};
+  DW hd[2][3];                 // head rows (a, b, c), double-word
+  DW td[2][3];                 // tail rows (a, b, c), double-word; td[nt-1] is row n-1
   double sigma0 = 1.0, sigmaN = 1.0;  // compact boundary RHS scales
   DW s;                               // output scale x = s * xi
   int unit_scale = 1;
   unsigned* status = nullptr;  // bit 0: input outside the FP32+refine range
 };
 
-template <int M>
+template <int M, bool DECAY>
 int refine_dispatch(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2,
                     int sweeps, int rhs, int W, cudaStream_t st);
 
@@ -75,7 +75,11 @@ __device__ __forceinline__ int tile_off(int r) {
 }
 
 // FP32 chunked LU solve, in place on v (RHS in, solution out); t is scratch.
-template <int M>
+// DECAY: the factor products over every chunk (prod |l|, prod |w| over M
+// rows) are below 2^-26, i.e. below FP32 rounding, so the carry entering a
+// chunk is the previous chunk's local end value alone and the carry scans
+// reduce to one shuffle each (the plan checks the products on the host).
+template <int M, bool DECAY>
 __device__ __forceinline__ void chunk_solve(float (&v)[M], float (&t)[M], const float* tl, const float* tg,
                                             const float* tw, unsigned lane) {
   float yh = 0.f, phi = 1.f;
@@ -87,14 +91,17 @@ __device__ __forceinline__ void chunk_solve(float (&v)[M], float (&t)[M], const 
     v[k] = yh;
     t[k] = phi;
   }
-  float A = phi, B = yh;
+  float B = yh;
+  if (!DECAY) {
+    float A = phi;
 #pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const float Ap = __shfl_up_sync(FULL, A, d);
-    const float Bp = __shfl_up_sync(FULL, B, d);
-    if (lane >= (unsigned)d) {
-      B = fmaf(A, Bp, B);
-      A = A * Ap;
+    for (int d = 1; d < 32; d <<= 1) {
+      const float Ap = __shfl_up_sync(FULL, A, d);
+      const float Bp = __shfl_up_sync(FULL, B, d);
+      if (lane >= (unsigned)d) {
+        B = fmaf(A, Bp, B);
+        A = A * Ap;
+      }
     }
   }
   float Yprev = __shfl_up_sync(FULL, B, 1);
@@ -109,14 +116,17 @@ __device__ __forceinline__ void chunk_solve(float (&v)[M], float (&t)[M], const 
     v[k] = xh;
     t[k] = psi;
   }
-  float A2 = psi, B2 = xh;
+  float B2 = xh;
+  if (!DECAY) {
+    float A2 = psi;
 #pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const float Ap = __shfl_down_sync(FULL, A2, d);
-    const float Bp = __shfl_down_sync(FULL, B2, d);
-    if (lane + d < 32u) {
-      B2 = fmaf(A2, Bp, B2);
-      A2 = A2 * Ap;
+    for (int d = 1; d < 32; d <<= 1) {
+      const float Ap = __shfl_down_sync(FULL, A2, d);
+      const float Bp = __shfl_down_sync(FULL, B2, d);
+      if (lane + d < 32u) {
+        B2 = fmaf(A2, Bp, B2);
+        A2 = A2 * Ap;
+      }
     }
   }
   float Xnext = __shfl_down_sync(FULL, B2, 1);
@@ -133,16 +143,16 @@ __device__ __forceinline__ void chunk_solve(float (&v)[M], float (&t)[M], const 
 // needed; the low-order terms are collected in the tail.
 template <bool POW2, bool HASLO>
 __device__ __forceinline__ float residual_row(float dh, float dl, float xm, float x0, float xp, float lm, float l0,
-                                              float lp, const RefineArgs& a) {
+                                              float lp, DW ca, DW cb, DW cc) {
   float pa, pb, pc, ea = 0.f, eb = 0.f, ec = 0.f;
   if (POW2) {
-    pa = __fmul_rn(a.ai.h, xm);
-    pb = __fmul_rn(a.bi.h, x0);
-    pc = __fmul_rn(a.ci.h, xp);
+    pa = __fmul_rn(ca.h, xm);
+    pb = __fmul_rn(cb.h, x0);
+    pc = __fmul_rn(cc.h, xp);
   } else {
-    two_prod(a.ai.h, xm, pa, ea);
-    two_prod(a.bi.h, x0, pb, eb);
-    two_prod(a.ci.h, xp, pc, ec);
+    two_prod(ca.h, xm, pa, ea);
+    two_prod(cb.h, x0, pb, eb);
+    two_prod(cc.h, xp, pc, ec);
   }
   float s, es, p, ep;
   two_sum(pa, pc, s, es);
@@ -150,19 +160,11 @@ __device__ __forceinline__ float residual_row(float dh, float dl, float xm, floa
   float tail = __fsub_rn(dl, __fadd_rn(ep, es));
   if (!POW2) {
     tail -= (ea + eb) + ec;
-    tail -= fmaf(a.ai.l, xm, fmaf(a.bi.l, x0, a.ci.l * xp));
+    tail -= fmaf(ca.l, xm, fmaf(cb.l, x0, cc.l * xp));
   }
-  if (HASLO) tail -= fmaf(a.ai.h, lm, fmaf(a.bi.h, l0, a.ci.h * lp));
+  if (HASLO) tail -= fmaf(ca.h, lm, fmaf(cb.h, l0, cc.h * lp));
   return __fadd_rn(__fsub_rn(dh, p), tail);
 }
-
-// FP64 residual of a special row from FP64 neighbours.
-__device__ __forceinline__ float residual_special(double d, double xm, double x0, double xp, double a, double b,
-                                                  double c) {
-  return (float)(d - (a * xm + b * x0 + c * xp));
-}
-
-__device__ __forceinline__ double head_a(const RefineArgs& a, int r) { return r == 0 ? 0.0 : a.ha[r]; }
 
 #ifndef NTK_REFINE_OCC
 #define NTK_REFINE_OCC 3
@@ -172,7 +174,7 @@ struct RefineOcc {
   static constexpr int value = (M <= 16) ? NTK_REFINE_OCC : 1;
 };
 
-template <int M, int RHS, int SWEEPS, bool POW2, bool PAD>
+template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY>
 __global__ void __launch_bounds__(256, RefineOcc<M>::value)
     refine_kernel(const double* in, double* out, int n, Batch b, RefineArgs ra) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -234,10 +236,16 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
       // D_r = f_{r+1} - f_{r-1} is formed in FP64 (one DADD, as in the FP64
       // path) and then split: a double-word split of f itself keeps only
       // ~2^-47 |f|, too coarse when f_{r+1} and f_{r-1} nearly cancel.
-      double dsp0 = 0.0, dsp1 = 0.0;  // one-sided boundary stencils (compact/rhs.py:21-31), FP64
-      if (j == 0) dsp0 = ra.sigma0 * ((-5.0 * trow[tile_off<M>(0)] + 4.0 * trow[tile_off<M>(1)]) + trow[tile_off<M>(2)]);
-      if (tail_here)
-        dsp1 = ra.sigmaN * ((-5.0 * trow[tile_off<M>(n1)] + 4.0 * trow[tile_off<M>(n1 - 1)]) + trow[tile_off<M>(n1 - 2)]);
+      // One-sided boundary stencils (compact/rhs.py:21-31) in FP64, evaluated
+      // once per warp: lane 0 evaluates row 0, the lane owning row n-1 that
+      // row, the other lanes a discarded copy (a divergent evaluation would
+      // cost the slow FP64 pipe a full warp instruction per row).
+      const int q0 = tail_here ? n1 : 0, q1 = tail_here ? n1 - 1 : 1, q2 = tail_here ? n1 - 2 : 2;
+      const double dsp = (tail_here ? ra.sigmaN : ra.sigma0) *
+                         ((-5.0 * trow[tile_off<M>(q0)] + 4.0 * trow[tile_off<M>(q1)]) + trow[tile_off<M>(q2)]);
+      double dsp0 = dsp, dsp1 = dsp;
+      if (j == 0 && tail_here)  // only when one lane holds the whole system
+        dsp0 = ra.sigma0 * ((-5.0 * trow[tile_off<M>(0)] + 4.0 * trow[tile_off<M>(1)]) + trow[tile_off<M>(2)]);
       const double fleft = (j > 0) ? trow[tile_off<M>(r0 - 1)] : 0.0;
       const double fright = (j < 31) ? trow[tile_off<M>(r0 + M)] : 0.0;
       __syncwarp();  // the neighbours' halo reads happen before any slot is rewritten
@@ -286,7 +294,7 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
 
     // ---- FP32 solve ----
     float tmp[M];
-    chunk_solve<M>(x, tmp, tl, tg, tw, lane);
+    chunk_solve<M, DECAY>(x, tmp, tl, tg, tw, lane);
 
     // ---- refinement sweeps ----
     float xl[M];
@@ -313,27 +321,30 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
         const float xm = (k == 0) ? xleft : x[k - (k > 0)];
         const float xp = (k == M - 1) ? xright : x[k + (k < M - 1)];
         if (sweep == 0) {
-          r[k] = residual_row<POW2, false>(d.x, d.y, xm, x[k], xp, 0.f, 0.f, 0.f, ra);
+          r[k] = residual_row<POW2, false>(d.x, d.y, xm, x[k], xp, 0.f, 0.f, 0.f, ra.ai, ra.bi, ra.ci);
         } else {
           const float lm = (k == 0) ? lleft : xl[k - (k > 0)];
           const float lp = (k == M - 1) ? lright : xl[k + (k < M - 1)];
-          r[k] = residual_row<POW2, true>(d.x, d.y, xm, x[k], xp, lm, xl[k], lp, ra);
+          r[k] = residual_row<POW2, true>(d.x, d.y, xm, x[k], xp, lm, xl[k], lp, ra.ai, ra.bi, ra.ci);
         }
       }
-      // head rows (lane 0, compile-time positions), FP64
+      // rows with their own coefficients, in double-word FP32 like the
+      // interior: head rows sit in lane 0 at compile-time positions
       if (j == 0) {
 #pragma unroll
         for (int k = 0; k < 2 && k < M; ++k) {
           if (k < ra.nh) {
             const float2 d = drow[cb + k];
-            const double xm = (k == 0) ? 0.0 : dw_to_f64(x[k - (k > 0)], xl[k - (k > 0)]);
-            const double xp = (k == M - 1) ? dw_to_f64(xright, lright) : dw_to_f64(x[k + (k < M - 1)], xl[k + (k < M - 1)]);
-            r[k] = residual_special((double)d.x + (double)d.y, xm, dw_to_f64(x[k], xl[k]), xp, head_a(ra, k),
-                                    ra.hb[k], ra.hc[k]);
+            const float xm = (k == 0) ? 0.f : x[k - (k > 0)];
+            const float lm = (k == 0) ? 0.f : xl[k - (k > 0)];
+            const float xp = (k == M - 1) ? xright : x[k + (k < M - 1)];
+            const float lp = (k == M - 1) ? lright : xl[k + (k < M - 1)];
+            r[k] = residual_row<false, true>(d.x, d.y, xm, x[k], xp, lm, xl[k], lp, ra.hd[k][0], ra.hd[k][1],
+                                             ra.hd[k][2]);
           }
         }
       }
-      // tail rows, FP64
+      // tail rows
       if (r0 + M > n - ra.nt && r0 < n) {
         if (!PAD) {
 #pragma unroll
@@ -342,10 +353,12 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
             if (q < ra.nt && k >= 0) {
               const int ti = ra.nt - 1 - q;
               const float2 d = drow[cb + k];
-              const double xm = (k == 0) ? dw_to_f64(xleft, lleft) : dw_to_f64(x[k - (k > 0)], xl[k - (k > 0)]);
-              const double xp = (q == 0) ? 0.0 : dw_to_f64(x[k + (k < M - 1)], xl[k + (k < M - 1)]);
-              r[k] = residual_special((double)d.x + (double)d.y, xm, dw_to_f64(x[k], xl[k]), xp, ra.ta[ti],
-                                      ra.tb[ti], (q == 0) ? 0.0 : ra.tc[ti]);
+              const float xm = (k == 0) ? xleft : x[k - (k > 0)];
+              const float lm = (k == 0) ? lleft : xl[k - (k > 0)];
+              const float xp = (q == 0) ? 0.f : x[k + (k < M - 1)];
+              const float lp = (q == 0) ? 0.f : xl[k + (k < M - 1)];
+              r[k] = residual_row<false, true>(d.x, d.y, xm, x[k], xp, lm, xl[k], lp, ra.td[ti][0], ra.td[ti][1],
+                                               ra.td[ti][2]);
             }
           }
         } else {
@@ -379,11 +392,14 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
                 xhp = xright;
                 xlp = lright;
               }
+              if (q == 0) {
+                xhp = 0.f;
+                xlp = 0.f;
+              }
               const int ti = ra.nt - 1 - q;
               const float2 d = drow[tile_off<M>(row)];
-              const float rr = residual_special((double)d.x + (double)d.y, dw_to_f64(xhm, xlm), dw_to_f64(xh0, xl0),
-                                                q == 0 ? 0.0 : dw_to_f64(xhp, xlp), ra.ta[ti], ra.tb[ti],
-                                                q == 0 ? 0.0 : ra.tc[ti]);
+              const float rr = residual_row<false, true>(d.x, d.y, xhm, xh0, xhp, xlm, xl0, xlp, ra.td[ti][0],
+                                                         ra.td[ti][1], ra.td[ti][2]);
 #pragma unroll
               for (int k = 0; k < M; ++k)
                 if (k == kk) r[k] = rr;
@@ -391,13 +407,24 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
           }
         }
       }
-      chunk_solve<M>(r, tmp, tl, tg, tw, lane);
+      chunk_solve<M, DECAY>(r, tmp, tl, tg, tw, lane);
+      if (sweep == 0) {
+        // x + delta exactly as a normalised double-word
 #pragma unroll
-      for (int k = 0; k < M; ++k) {
-        float h, e;
-        two_sum(x[k], r[k], h, e);
-        e += xl[k];
-        fast_two_sum(h, e, x[k], xl[k]);
+        for (int k = 0; k < M; ++k) {
+          float h, e;
+          two_sum(x[k], r[k], h, e);
+          x[k] = h;
+          xl[k] = e;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < M; ++k) {
+          float h, e;
+          two_sum(x[k], r[k], h, e);
+          e += xl[k];
+          fast_two_sum(h, e, x[k], xl[k]);
+        }
       }
     }
 
@@ -450,10 +477,10 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
   }
 }
 
-template <int M, int RHS, int SWEEPS, bool POW2, bool PAD>
+template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY>
 int launch_one(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, int W, cudaStream_t st) {
   const size_t smem = (size_t)W * sys_pitch<M>() * sizeof(double) + 3 * 32 * (M + 1) * sizeof(float);
-  auto kern = refine_kernel<M, RHS, SWEEPS, POW2, PAD>;
+  auto kern = refine_kernel<M, RHS, SWEEPS, POW2, PAD, DECAY>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(refine_kernel)");
   const long long blocks = (b.nsys + W - 1) / W;
@@ -461,35 +488,37 @@ int launch_one(const double* in, double* out, int n, const Batch& b, const Refin
   return cuda_status(cudaGetLastError(), "refine_kernel");
 }
 
-template <int M, int RHS, int SWEEPS>
+template <int M, int RHS, int SWEEPS, bool DECAY>
 int dispatch_pp(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2, int W,
                 cudaStream_t st) {
   const bool pad = (n != 32 * M);
   if (pow2)
-    return pad ? launch_one<M, RHS, SWEEPS, true, true>(in, out, n, b, ra, W, st)
-               : launch_one<M, RHS, SWEEPS, true, false>(in, out, n, b, ra, W, st);
-  return pad ? launch_one<M, RHS, SWEEPS, false, true>(in, out, n, b, ra, W, st)
-             : launch_one<M, RHS, SWEEPS, false, false>(in, out, n, b, ra, W, st);
+    return pad ? launch_one<M, RHS, SWEEPS, true, true, DECAY>(in, out, n, b, ra, W, st)
+               : launch_one<M, RHS, SWEEPS, true, false, DECAY>(in, out, n, b, ra, W, st);
+  return pad ? launch_one<M, RHS, SWEEPS, false, true, DECAY>(in, out, n, b, ra, W, st)
+             : launch_one<M, RHS, SWEEPS, false, false, DECAY>(in, out, n, b, ra, W, st);
 }
 
-template <int M, int RHS>
+template <int M, int RHS, bool DECAY>
 int dispatch_sweeps(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2,
                     int sweeps, int W, cudaStream_t st) {
   switch (sweeps) {
-    case 0: return dispatch_pp<M, RHS, 0>(in, out, n, b, ra, pow2, W, st);
-    case 1: return dispatch_pp<M, RHS, 1>(in, out, n, b, ra, pow2, W, st);
-    default: return dispatch_pp<M, RHS, 2>(in, out, n, b, ra, pow2, W, st);
+    case 0: return dispatch_pp<M, RHS, 0, DECAY>(in, out, n, b, ra, pow2, W, st);
+    case 1: return dispatch_pp<M, RHS, 1, DECAY>(in, out, n, b, ra, pow2, W, st);
+    default: return dispatch_pp<M, RHS, 2, DECAY>(in, out, n, b, ra, pow2, W, st);
   }
 }
 
 }  // namespace refine_detail
 
-template <int M>
+// Kernel instances for one M and one carry mode (DECAY); the ntk_refine_m*.cu
+// translation units instantiate them, ntk_refine.cu picks one.
+template <int M, bool DECAY>
 int refine_dispatch(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2,
                     int sweeps, int rhs, int W, cudaStream_t st) {
   using namespace refine_detail;
-  if (rhs == RHS_COMPACT) return dispatch_sweeps<M, RHS_COMPACT>(in, out, n, b, ra, pow2, sweeps, W, st);
-  return dispatch_sweeps<M, RHS_IDENTITY>(in, out, n, b, ra, pow2, sweeps, W, st);
+  if (rhs == RHS_COMPACT) return dispatch_sweeps<M, RHS_COMPACT, DECAY>(in, out, n, b, ra, pow2, sweeps, W, st);
+  return dispatch_sweeps<M, RHS_IDENTITY, DECAY>(in, out, n, b, ra, pow2, sweeps, W, st);
 }
 
 }  // namespace ntk

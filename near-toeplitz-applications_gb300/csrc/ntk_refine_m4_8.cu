@@ -1,0 +1,9 @@
+// ntk_refine_m4_8.cu -- kernel instances of ntk_refine.cuh (one TU per M and carry mode, for parallel builds).
+#include "ntk_refine.cuh"
+
+namespace ntk {
+template int refine_dispatch<4, false>(const double*, double*, int, const Batch&, const RefineArgs&, bool, int,
+                                          int, int, cudaStream_t);
+template int refine_dispatch<8, false>(const double*, double*, int, const Batch&, const RefineArgs&, bool, int,
+                                          int, int, cudaStream_t);
+}  // namespace ntk

@@ -392,10 +392,161 @@ __global__ void __launch_bounds__(32) thomas_f64_staged_kernel(const double* __r
   }
 }
 
+// ----------------------------------------------------------------------------
+// contiguous (x-direction) systems, many at a time: each warp takes 32
+// adjacent systems and moves their rows through a per-warp ring of 32 x 33
+// shared-memory tiles.  Loads and stores touch one system's 32 consecutive
+// rows per instruction (coalesced 256 B), the recurrence reads the tile
+// transposed (lane = system; pitch 33 keeps both directions conflict-free).
+// cp.async keeps the next tiles in flight while the current one is solved.
+// Forward: f tiles in, eta tiles out (parked in `out`); backward: eta tiles
+// in, x tiles out.  Needs es == 1 and the 32 systems of a warp to be
+// equally spaced (is), which the launcher checks.
+// ----------------------------------------------------------------------------
+constexpr int XT = 32;       // rows per tile
+constexpr int XP = XT + 1;   // tile pitch (doubles)
+constexpr int XRING = 3;     // tiles in flight per warp
+constexpr int XWARPS = 4;    // warps per CTA
+
+__device__ __forceinline__ void xtile_issue(double* tile, const double* base0, long long is, int cnt, int row0, int n,
+                                            int lane) {
+  const int r = row0 + lane;
+  const bool ok = r < n;
+#pragma unroll 8
+  for (int w = 0; w < 32; ++w) {
+    const bool v = ok && (w < cnt);
+    cp_async8(tile + lane * XP + w, base0 + (v ? (long long)w * is + r : 0), v ? 8u : 0u);
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void xtile_store(const double* tile, double* base0, long long is, int cnt, int row0, int n,
+                                            int lane) {
+  const int r = row0 + lane;
+  if (r < n) {
+#pragma unroll 8
+    for (int w = 0; w < 32; ++w)
+      if (w < cnt) base0[(long long)w * is + r] = tile[lane * XP + w];
+  }
+}
+
+template <int RHS>
+__global__ void __launch_bounds__(XT * XWARPS) thomas_f64_xpose_kernel(const double* in, double* out, int n, Batch b,
+                                                                       RhsParams rp, TablesF64 t) {
+  extern __shared__ __align__(16) double xsm[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  double* ring = xsm + (size_t)warp * XRING * XT * XP;
+  const long long s0 = ((long long)blockIdx.x * XWARPS + warp) * 32;
+  if (s0 >= b.nsys) return;  // whole warp
+  const int cnt = (int)min(32LL, b.nsys - s0);
+  const long long off0 = (s0 / b.ni) * b.os + (s0 % b.ni) * b.is;
+  const double* src = in + off0;
+  double* dst = out + off0;
+  const int C = (n + XT - 1) / XT;
+
+  // ---- forward: eta_i, tiles of f in, tiles of eta out ----
+  double eta = 0.0;
+  double fm = 0.0, fc = 0.0;  // compact: f_{i-1}, f_i
+  double fl0 = 0.0, fl1 = 0.0, fl2 = 0.0;
+  xtile_issue(ring, src, b.is, cnt, 0, n, lane);
+  if (C > 1) xtile_issue(ring + XT * XP, src, b.is, cnt, XT, n, lane);
+  for (int c = 0; c < C; ++c) {
+    double* cur = ring + (c % XRING) * XT * XP;
+    const double* nxt = ring + ((c + 1) % XRING) * XT * XP;
+    // tiles c and c+1 must be complete (the compact RHS of the tile's last
+    // row needs the next tile's first row); only tile c+2 may stay in flight
+    if (c + 2 < C) {
+      xtile_issue(ring + ((c + 2) % XRING) * XT * XP, src, b.is, cnt, (c + 2) * XT, n, lane);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
+    __syncwarp();
+    const int row0 = c * XT;
+    const int rows = min(XT, n - row0);
+    if constexpr (RHS == RHS_IDENTITY) {
+#pragma unroll 8
+      for (int k = 0; k < rows; ++k) {
+        const int i = row0 + k;
+        const double v = cur[k * XP + lane];
+        eta = (i == 0) ? v : fma(-__ldg(t.l + i), eta, v);
+        cur[k * XP + lane] = eta;
+      }
+    } else {
+      if (c == 0) {
+        fm = cur[0 * XP + lane];
+        fc = cur[1 * XP + lane];
+        eta = rp.sigma0 * ((-5.0 * fm + 4.0 * fc) + cur[2 * XP + lane]);
+      }
+#pragma unroll 8
+      for (int k = 0; k < rows; ++k) {
+        const int i = row0 + k;
+        if (i == 0) {
+          cur[lane] = eta;
+          continue;
+        }
+        if (i == n - 1) {
+          eta = fma(-__ldg(t.l + i), eta, rp.sigmaN * ((-5.0 * fl2 + 4.0 * fl1) + fl0));
+          cur[k * XP + lane] = eta;
+          continue;
+        }
+        // f_{i+1}: next row of this tile or the first row of the next tile
+        const double fp = (k + 1 < XT) ? cur[(k + 1) * XP + lane] : nxt[lane];
+        if (i == n - 3) fl0 = fc;
+        eta = fma(-__ldg(t.l + i), eta, fp - fm);
+        fm = fc;
+        fc = fp;
+        if (i == n - 2) {
+          fl1 = fm;
+          fl2 = fc;
+        }
+        cur[k * XP + lane] = eta;
+      }
+    }
+    __syncwarp();
+    xtile_store(cur, dst, b.is, cnt, row0, n, lane);
+    __syncwarp();
+  }
+  // ---- backward: x_i = g_i eta_i - w_i x_{i+1}, tiles of eta in (from out) ----
+  // each lane reads back exactly the rows it stored; the fence orders those
+  // stores before the asynchronous copies that read them
+  __threadfence_block();
+  double x = 0.0;
+  xtile_issue(ring, dst, b.is, cnt, (C - 1) * XT, n, lane);
+  if (C > 1) xtile_issue(ring + XT * XP, dst, b.is, cnt, (C - 2) * XT, n, lane);
+  for (int cc = 0; cc < C; ++cc) {
+    const int c = C - 1 - cc;
+    double* cur = ring + (cc % XRING) * XT * XP;
+    if (cc + 2 < C) {
+      xtile_issue(ring + ((cc + 2) % XRING) * XT * XP, dst, b.is, cnt, (c - 2) * XT, n, lane);
+      asm volatile("cp.async.wait_group 2;\n" ::: "memory");
+    } else if (cc + 1 < C) {
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
+    __syncwarp();
+    const int row0 = c * XT;
+    const int rows = min(XT, n - row0);
+#pragma unroll 8
+    for (int k = rows - 1; k >= 0; --k) {
+      const int i = row0 + k;
+      const double e = cur[k * XP + lane];
+      x = (i == n - 1) ? __ldg(t.g + i) * e : fma(-__ldg(t.w + i), x, __ldg(t.g + i) * e);
+      cur[k * XP + lane] = x;
+    }
+    __syncwarp();
+    xtile_store(cur, dst, b.is, cnt, row0, n, lane);
+    __syncwarp();
+  }
+
+}
+
 }  // namespace
 
 int launch_thomas_f64(const double* in, double* out, int n, const Batch& b, const RhsParams& rp,
-                      const TablesF64& t, int threads, cudaStream_t stream) {
+                      const TablesF64& t, int threads, cudaStream_t stream, int x_variant) {
   if (b.nsys <= 0) return NTK_OK;
   if (threads <= 0 || threads > 128 || threads % 32) threads = 128;
   const long long blocks = (b.nsys + threads - 1) / threads;
@@ -407,10 +558,27 @@ int launch_thomas_f64(const double* in, double* out, int n, const Batch& b, cons
   bool vec = (b.es == 1) && (n % 2 == 0) && (b.is % 2 == 0) && (b.os % 2 == 0) &&
              ((reinterpret_cast<uintptr_t>(in) & 15) == 0) && ((reinterpret_cast<uintptr_t>(out) & 15) == 0);
   dim3 grid((unsigned)blocks), block(threads);
+  // contiguous systems, 32 per warp equally spaced: transposing tile ring
+  const bool xlike = (b.es == 1) && (b.ni >= b.nsys || b.ni % 32 == 0) && (rp.kind == RHS_IDENTITY || n >= 4) &&
+                     (rp.kind == RHS_IDENTITY || rp.kind == RHS_COMPACT);
+  if (xlike && x_variant == 0) {
+    const size_t xs = (size_t)XWARPS * XRING * XT * XP * sizeof(double);
+    const long long xblocks = (b.nsys + 32 * XWARPS - 1) / (32 * XWARPS);
+    if (rp.kind == RHS_IDENTITY) {
+      auto k = thomas_f64_xpose_kernel<RHS_IDENTITY>;
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs);
+      k<<<(unsigned)xblocks, XT * XWARPS, xs, stream>>>(in, out, n, b, rp, t);
+    } else {
+      auto k = thomas_f64_xpose_kernel<RHS_COMPACT>;
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs);
+      k<<<(unsigned)xblocks, XT * XWARPS, xs, stream>>>(in, out, n, b, rp, t);
+    }
+    return cuda_status(cudaGetLastError(), "thomas_f64_xpose_kernel");
+  }
   // contiguous systems that fit a 32-system tile in shared memory: staged kernel
   const size_t smem = (size_t)32 * (n + 1) * sizeof(double);
   if (b.es == 1 && smem <= 200 * 1024 && (rp.kind == RHS_IDENTITY || rp.kind == RHS_COMPACT) &&
-      (rp.kind == RHS_IDENTITY || n >= 4)) {
+      (rp.kind == RHS_IDENTITY || n >= 4) && x_variant != 2) {
     const long long sblocks = (b.nsys + 31) / 32;
     if (rp.kind == RHS_IDENTITY) {
       auto k = thomas_f64_staged_kernel<RHS_IDENTITY>;

@@ -144,6 +144,21 @@ class Plan:
     def __exit__(self, *exc):
         self.close()
 
+    def set_tuning(self, **kw):
+        """Set launch parameters: f64_x_variant, f64_threads, refine_w."""
+        for k, v in kw.items():
+            if k not in _lib.TUNE_KEYS:
+                raise ValueError("unknown tuning key %r" % k)
+            check(load().ntk_plan_set_tuning(self.handle, _lib.TUNE_KEYS[k], int(v)))
+
+    def get_tuning(self):
+        out = {}
+        for k, key in _lib.TUNE_KEYS.items():
+            v = ctypes.c_int()
+            check(load().ntk_plan_get_tuning(self.handle, key, ctypes.byref(v)))
+            out[k] = v.value
+        return out
+
     def solve(self, d, stream=None):
         """In-place solve of nrhs contiguous systems starting at d (neato.py:168-197)."""
         ne = _available(d)

@@ -24,6 +24,12 @@ NTK_FP32_REFINE = 2
 
 PRECISIONS = {"fp64": NTK_FP64, "fp32": NTK_FP32, "fp32_refine": NTK_FP32_REFINE}
 
+NTK_TUNE_F64_X_VARIANT = 1
+NTK_TUNE_F64_THREADS = 2
+NTK_TUNE_REFINE_W = 3
+TUNE_KEYS = {"f64_x_variant": NTK_TUNE_F64_X_VARIANT, "f64_threads": NTK_TUNE_F64_THREADS,
+             "refine_w": NTK_TUNE_REFINE_W}
+
 # (name, restype, argtypes) of every exported entry point, in header order
 _vp = ctypes.c_void_p
 _i = ctypes.c_int
@@ -33,6 +39,8 @@ SIGNATURES = [
     ("ntk_version", ctypes.c_char_p, []),
     ("ntk_last_error", _i, [ctypes.c_char_p, _i]),
     ("ntk_plan_create", _i, [ctypes.POINTER(_vp), _i, _ll, ctypes.POINTER(_d), _i, _i]),
+    ("ntk_plan_set_tuning", _i, [_vp, _i, _i]),
+    ("ntk_plan_get_tuning", _i, [_vp, _i, ctypes.POINTER(_i)]),
     ("ntk_plan_destroy", _i, [_vp]),
     ("ntk_solve", _i, [_vp, _vp, _vp]),
     ("ntk_solve_strided", _i, [_vp, _vp, _vp, _ll, _ll, _ll, _ll, _ll, _vp]),

@@ -98,3 +98,11 @@ def test_missing_library_fails_loudly(tmp_path):
 
     with pytest.raises(RuntimeError, match="libntk.so not found"):
         _lib.load(str(tmp_path / "libntk.so"))
+
+
+def test_tuning_keys_validated(ntk_lib):
+    from ntk import _lib
+
+    v = ctypes.c_int()
+    assert ntk_lib.ntk_plan_set_tuning(None, 1, 0) == _lib.NTK_ERR_INVALID
+    assert ntk_lib.ntk_plan_get_tuning(None, 1, ctypes.byref(v)) == _lib.NTK_ERR_INVALID

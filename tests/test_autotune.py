@@ -1,0 +1,65 @@
+"""Autotuner logic on the CPU (fake plan, fake timer) and on the GPU."""
+import numpy as np
+import pytest
+
+
+class FakePlan:
+    def __init__(self, precision):
+        self.n = 512
+        self.precision = precision
+        self.cfg = {}
+
+    def set_tuning(self, **kw):
+        self.cfg.update(kw)
+
+
+def test_candidates_cover_the_space():
+    from ntk import autotune
+
+    c = autotune.candidates("fp64")
+    assert {"f64_x_variant": 0, "f64_threads": 64} in c and len(c) == 4
+    assert autotune.candidates("fp32_refine") == [{"refine_w": 4}, {"refine_w": 8}]
+
+
+def test_tune_picks_fastest_and_caches(tmp_path, monkeypatch):
+    from ntk import autotune
+
+    monkeypatch.setenv("NTK_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
+    monkeypatch.setattr(autotune, "device_name", lambda: "FAKE-GPU")
+    plan = FakePlan("fp32_refine")
+    fake_ms = {4: 2.0, 8: 1.0}
+
+    def timer(run, repeats):
+        return fake_ms[plan.cfg["refine_w"]]
+
+    res = autotune.tune(plan, lambda: None, key="compact-x", timer=timer)
+    assert res["config"] == {"refine_w": 8} and plan.cfg["refine_w"] == 8
+    plan2 = FakePlan("fp32_refine")
+    assert autotune.apply_cached(plan2, "compact-x") == {"refine_w": 8}
+    assert plan2.cfg == {"refine_w": 8}
+    # a cache hit does not time again
+    res2 = autotune.tune(FakePlan("fp32_refine"), lambda: None, key="compact-x",
+                         timer=lambda *a: pytest.fail("timed despite cache"))
+    assert res2["config"] == {"refine_w": 8}
+
+
+@pytest.mark.gpu
+def test_tune_on_gpu_keeps_results_correct(cuda, oracle, tmp_path, monkeypatch):
+    import torch
+
+    import ntk
+    from ntk import autotune
+
+    monkeypatch.setenv("NTK_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
+    n = 256
+    f = np.random.default_rng(0).normal(size=(8, 64, n))
+    ft = torch.from_numpy(f).to(cuda)
+    out = torch.empty_like(ft)
+    for prec, tol in (("fp64", 1e-13), ("fp32_refine", 1e-12)):
+        with ntk.Plan(n, 0, ntk.COMPACT_COEFFS, precision=prec) as p:
+            res = autotune.tune(p, lambda: p.compact_deriv(ft, out, axis=2, h=0.01), key="t")
+            cur = p.get_tuning()
+            assert all(cur[k] == v for k, v in res["config"].items())
+            p.compact_deriv(ft, out, axis=2, h=0.01)
+            torch.cuda.synchronize()
+        assert oracle.rel_err(out.cpu().numpy(), oracle.banded_compact_deriv(f, 0.01, 2)) < tol

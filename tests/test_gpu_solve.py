@@ -177,3 +177,44 @@ def test_strided_solve_matches_contiguous(cuda, oracle):
         ref = oracle.cr_solve(np.ascontiguousarray(np.transpose(d, (0, 2, 1))), ny, co)
         got = np.transpose(out.cpu().numpy(), (0, 2, 1))
         assert oracle.rel_err(got, ref) < tol
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("n", [4, 33, 512, 700])
+def test_fp64_x_variants(cuda, oracle, variant, n):
+    """Every launch variant of the contiguous FP64 sweep gives the same solve
+    (and the fused compact derivative)."""
+    import ntk
+
+    co = COEFF_SETS["compact"]
+    nrhs = 70
+    d = np.random.default_rng(n + variant).normal(size=(nrhs, n))
+    t = torch.from_numpy(d).to(cuda)
+    with ntk.Plan(n, nrhs, co) as p:
+        p.set_tuning(f64_x_variant=variant)
+        assert p.get_tuning()["f64_x_variant"] == variant
+        p.solve(t)
+        torch.cuda.synchronize()
+    assert oracle.rel_err(t.cpu().numpy(), _banded(oracle, n, co, d)) < FP64_TOL
+    f = np.random.default_rng(n).normal(size=(3, nrhs // 3, n))
+    ft = torch.from_numpy(f).to(cuda)
+    out = torch.empty_like(ft)
+    with ntk.Plan(n, 0, co) as p:
+        p.set_tuning(f64_x_variant=variant)
+        p.compact_deriv(ft, out, axis=2, h=0.1)
+        torch.cuda.synchronize()
+    assert oracle.rel_err(out.cpu().numpy(), oracle.banded_compact_deriv(f, 0.1, 2)) < FP64_TOL
+
+
+@pytest.mark.parametrize("w", [4, 8])
+def test_refine_w_tuning(cuda, oracle, w):
+    import ntk
+
+    co = COEFF_SETS["compact"]
+    d = np.random.default_rng(w).normal(size=(37, 512))
+    t = torch.from_numpy(d).to(cuda)
+    with ntk.Plan(512, 37, co, precision="fp32_refine") as p:
+        p.set_tuning(refine_w=w)
+        p.solve(t)
+        torch.cuda.synchronize()
+    assert oracle.rel_err(t.cpu().numpy(), _banded(oracle, 512, co, d)) < REFINE_TOL
