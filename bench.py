@@ -158,10 +158,10 @@ def _cpu_worker(task):
 
     import oracle as O
 
-    axis, lines, seed = task
+    axis, lines, seed, reps = task
     rng = np.random.default_rng(seed)
-    # `lines` complete lines of length N along `axis` from a 512^3 Fourier
-    # field sample: a [lines][N] slab built with the generator's modes
+    # `lines` complete lines of length N along `axis` of the 512^3 Fourier
+    # field (the generator's modes, random positions in the other two axes)
     from ntk.workloads import fourier_modes
 
     amps, ks, phases = fourier_modes(3, seed=0)
@@ -174,19 +174,23 @@ def _cpu_worker(task):
         arg = 2 * np.pi * (kk[axis] * g[None, :] + kk[other[0]] * pos[:, 0:1] + kk[other[1]] * pos[:, 1:2] + p)
         f += a * np.sin(arg)
     h = 1.0 / (N - 1)
+    fT = np.ascontiguousarray(f.T.reshape(N, lines, 1))
     t0 = time.perf_counter()
-    x = O.banded_compact_deriv(f.T.reshape(N, lines, 1), h, axis=0)
+    acc = 0.0
+    for _ in range(reps):
+        x = O.banded_compact_deriv(fT, h, axis=0)  # RHS + banded solve, timed
+        acc += float(x[0, 0, 0])
     dt = time.perf_counter() - t0
-    return dt, lines * N, float(np.abs(x).sum())
+    return dt, lines * N * reps, acc
 
 
-def cpu_path_rate(lines_per_task, tasks, processes):
+def cpu_path_rate(lines_per_task, tasks, processes, reps=1):
     """rows/s of the reference CPU path (RHS + banded solve, field generation
     excluded) on `processes` concurrent worker processes: total rows over the
     per-process solve time."""
     import multiprocessing as mp
 
-    jobs = [((t % 3), lines_per_task, 1000 + t) for t in range(tasks)]
+    jobs = [((t % 3), lines_per_task, 1000 + t, reps) for t in range(tasks)]
     if processes == 1:
         res = [_cpu_worker(j) for j in jobs]
     else:
@@ -253,6 +257,7 @@ def run_gpu(args):
 
     def step(plan):
         for axis in (2, 1, 0):
+            apply(plan, plan.precision, axis)
             plan.compact_deriv(f, outs[2 - axis], axis=axis, h=h)
 
     def timed(plan, steps, warmup, per_launch=False):
@@ -268,6 +273,7 @@ def run_gpu(args):
         for _ in range(steps):
             if per_launch:
                 for axis in (2, 1, 0):
+                    apply(plan, plan.precision, axis)
                     a = torch.cuda.Event(enable_timing=True)
                     b = torch.cuda.Event(enable_timing=True)
                     a.record(stream)
@@ -284,6 +290,19 @@ def run_gpu(args):
         for axis, a, b in ev:
             per.setdefault(axis, []).append(a.elapsed_time(b))
         return ms, {ax: sum(v) / len(v) for ax, v in per.items()}
+
+    # launch parameters per axis from the autotuner (timed once, then cached)
+    from ntk import autotune
+
+    tuned = {}
+    for p in ("fp64", "fp32", "fp32_refine"):
+        for axis in (2, 1, 0):
+            res = autotune.tune(plans[p], lambda p=p, axis=axis: plans[p].compact_deriv(f, outs[0], axis=axis, h=h),
+                                key="compact512-axis%d" % axis, repeats=3)
+            tuned[(p, axis)] = res["config"]
+
+    def apply(plan, prec, axis):
+        plan.set_tuning(**tuned[(prec, axis)])
 
     # accuracy (rank 0): refine and FP32 against the FP64 solve, and the
     # FP64 solve against the FP64 banded oracle on sampled lines
@@ -313,30 +332,57 @@ def run_gpu(args):
     ms_main = max_over_ranks(ms_main, world, dev)
     ms_fp64 = max_over_ranks(ms_fp64, world, dev)
 
-    # end to end through the public API: pinned host f in, three derivatives out
+    # end to end through the public API: every step copies the field in from
+    # pinned host memory and the three derivatives back out.  Copies and
+    # solves of consecutive steps overlap on three streams (H2D, compute,
+    # D2H) with double-buffered device arrays; the timed region runs from the
+    # first H2D to the last D2H.
     hf = torch.empty((N, N, N), dtype=torch.float64, pin_memory=True)
     hf.copy_(f)
     houts = [torch.empty((N, N, N), dtype=torch.float64, pin_memory=True) for _ in range(3)]
-    fd = torch.empty_like(f)
+    fds = [f, torch.empty_like(f)]
+    ods = [outs, [torch.empty_like(f) for _ in range(3)]]
+    s_in = torch.cuda.Stream(dev)
+    s_out = torch.cuda.Stream(dev)
+    done_comp = [None, None]
+    done_out = [None, None]
 
-    def e2e_step():
-        fd.copy_(hf, non_blocking=True)
+    def e2e_step(k):
+        slot = k % 2
+        with torch.cuda.stream(s_in):
+            if done_comp[slot] is not None:
+                s_in.wait_event(done_comp[slot])  # the buffer's previous solve has read it
+            fds[slot].copy_(hf, non_blocking=True)
+            ev_in = torch.cuda.Event()
+            ev_in.record(s_in)
+        stream.wait_event(ev_in)
+        if done_out[slot] is not None:
+            stream.wait_event(done_out[slot])  # previous results of this slot are out
         for axis in (2, 1, 0):
-            main.compact_deriv(fd, outs[2 - axis], axis=axis, h=h)
-        for i in range(3):
-            houts[i].copy_(outs[i], non_blocking=True)
+            apply(main, args.precision, axis)
+            main.compact_deriv(fds[slot], ods[slot][2 - axis], axis=axis, h=h, stream=stream)
+        ev_c = torch.cuda.Event()
+        ev_c.record(stream)
+        done_comp[slot] = ev_c
+        with torch.cuda.stream(s_out):
+            s_out.wait_event(ev_c)
+            for i in range(3):
+                houts[i].copy_(ods[slot][i], non_blocking=True)
+            ev_o = torch.cuda.Event()
+            ev_o.record(s_out)
+            done_out[slot] = ev_o
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
+    for k in range(max(2, args.warmup)):
+        e2e_step(k)
     torch.cuda.synchronize(dev)
     barrier(world, dev)
+    e2e_steps = max(4, args.steps // 4)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    e2e_steps = max(2, args.steps // 2)
-    for _ in range(e2e_steps):
-        e2e_step()
-    e1.record(stream)
+    e0.record(s_in)
+    for k in range(e2e_steps):
+        e2e_step(k)
+    e1.record(s_out)
     torch.cuda.synchronize(dev)
     ms_e2e = max_over_ranks(e0.elapsed_time(e1) / e2e_steps, world, dev)
 
@@ -352,10 +398,11 @@ def run_gpu(args):
     traffic = profile_traffic("refine_kernel_512cube" if args.precision != "fp64" else "thomas_f64_512cube")
     cpu = None
     if not args.no_cpu_baseline:
-        rate, rows, wall = cpu_path_rate(4096, 24, 1)
+        rate, rows, wall = cpu_path_rate(4096, 3, 1, reps=40)
         cpu = {"value": rate, "unit": "rows/s", "cores": 1, "kind": "port",
-               "sample": "%d systems of n=512 (x, y, z lines of the 512^3 field), numpy RHS + scipy "
-                         "solve_banded (experiments/run-compact.py:14-28), 1 process, %.1f s" % (rows // N, wall)}
+               "sample": "%d system solves of n=512 (x, y, z lines of the 512^3 field), numpy RHS + scipy "
+                         "solve_banded (experiments/run-compact.py:14-28), 1 process, %.1f s of CPU time"
+                         % (rows // N, wall)}
     line = {
         "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_main, "higher_is_better": True, "scaling": "weak",
@@ -365,7 +412,8 @@ def run_gpu(args):
         "data": "synthetic",
         "config": {"workload": "compact4 derivative x,y,z of a 512^3 FP64 field (3 x 262144 systems, n=512)",
                    "precision": args.precision, "refine_sweeps": args.sweeps,
-                   "l2": "1 GiB input > 129 MB L2 (no flush)", "parallelism": "replicas x%d" % world},
+                   "l2": "1 GiB input > 129 MB L2 (no flush)", "parallelism": "replicas x%d" % world,
+                   "tuning": {"%s/%s" % (p, "xyz"[2 - a]): c for (p, a), c in tuned.items()}},
         "fp64": {"ms_per_step": ms_fp64, "rows_per_s": world * ROWS_PER_STEP / (ms_fp64 * 1e-3),
                  "hbm_frac": (BYTES_PER_ROW * N ** 3 / (per_axis64[max(per_axis64, key=per_axis64.get)] * 1e-3) / 1e9)
                  / hbm},
@@ -418,16 +466,45 @@ def sample_oracle_errors(f, ref, h, lines=256):
     return {"fp64_vs_banded_oracle": worst}
 
 
+def profile_case(which):
+    """Small launches of the hot kernels for `ncu` (no timing): x on a
+    128 x 512 x 512 field, z on 512 x 256 x 256, one warm-up + one launch."""
+    import torch
+
+    import ntk
+    from ntk.workloads import COMPACT_COEFFS, fourier_field
+
+    dev = torch.device("cuda", 0)
+    fx = fourier_field((128, 512, 512), seed=0, device=dev)
+    fz = fourier_field((512, 256, 256), seed=0, device=dev)
+    for w in which:
+        prec, ax = w.split("_")
+        axis = {"x": 2, "y": 1, "z": 0}[ax]
+        f = fz if ax == "z" else fx
+        out = torch.empty_like(f)
+        n = f.shape[axis]
+        with ntk.Plan(n, 0, COMPACT_COEFFS, precision={"refine": "fp32_refine", "fp64": "fp64"}[prec]) as p:
+            for _ in range(2):
+                p.compact_deriv(f, out, axis=axis, h=1.0 / (n - 1))
+        torch.cuda.synchronize()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ntk", choices=["ntk", "reference"])
     ap.add_argument("--precision", default="fp32_refine", choices=["fp64", "fp32", "fp32_refine"])
     ap.add_argument("--sweeps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", default=None,
+                    help="comma list of refine_x,refine_z,fp64_x,fp64_z: two launches each on ~256 MiB fields "
+                         "(n = 512 along the solved axis), for ncu captures; prints nothing to time")
     args = ap.parse_args()
+    if args.profile_case:
+        return profile_case(args.profile_case.split(","))
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -54,19 +54,32 @@ int Plan::init_refine() {
   }
   st->M = M;
   st->n_pad = 32 * M;
-  // FP32 factor tables in the padded chunk layout; rows >= n are identity
-  std::vector<float> tab(3 * 32 * (M + 1), 0.f);
-  for (int r = 0; r < 32 * M; ++r) {
-    const int j = r / M, k = r % M;
-    float l = 0.f, g = 1.f, w = 0.f;
-    if (r < n) {
-      l = (float)lu_l[r];
-      g = (float)(1.0 / lu_u[r]);
-      w = (float)((r < n - 1 ? mat.c(r) : 0.0) / lu_u[r]);
+  // FP32 tables in the padded chunk layout (ChunkTabs); rows >= n are
+  // identity rows (l = w = 0, g = 1)
+  const int TS = 32 * (M + 1);
+  std::vector<double> L(32 * M, 0.0), G(32 * M, 1.0), Wv(32 * M, 0.0);
+  for (int r = 0; r < n; ++r) {
+    L[r] = lu_l[r];
+    G[r] = 1.0 / lu_u[r];
+    Wv[r] = (r < n - 1 ? mat.c(r) : 0.0) / lu_u[r];
+  }
+  std::vector<float> tab(6 * (size_t)TS, 0.f);  // gwp[TS] (4 floats each) | l[TS] | psi[TS]
+  for (int j = 0; j < 32; ++j) {
+    double phi = 1.0;
+    for (int k = 0; k < M; ++k) {
+      const int r = j * M + k, e = j * (M + 1) + k;
+      phi *= -L[r];
+      tab[4 * e + 0] = (float)G[r];
+      tab[4 * e + 1] = (float)Wv[r];
+      tab[4 * e + 2] = (float)phi;
+      tab[4 * TS + e] = (float)L[r];
     }
-    tab[0 * 32 * (M + 1) + j * (M + 1) + k] = l;
-    tab[1 * 32 * (M + 1) + j * (M + 1) + k] = g;
-    tab[2 * 32 * (M + 1) + j * (M + 1) + k] = w;
+    double psi = 1.0;
+    for (int k = M - 1; k >= 0; --k) {
+      const int r = j * M + k, e = j * (M + 1) + k;
+      psi *= -Wv[r];
+      tab[5 * TS + e] = (float)psi;
+    }
   }
   int rc = cuda_status(cudaMalloc(&st->d_tab, tab.size() * sizeof(float)), "cudaMalloc(refine tables)");
   if (rc) return rc;

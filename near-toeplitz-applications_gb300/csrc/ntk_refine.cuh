@@ -46,7 +46,7 @@ struct DW {
 };
 
 struct RefineArgs {
-  const float* tab = nullptr;  // [3][32][M+1]: l, g = 1/u, w = c/u (padded chunk layout)
+  const float* tab = nullptr;  // per padded row: [gwp float4][l][psi] (see ChunkTabs)
   DW ai, bi, ci;               // interior row coefficients
   int nh = 1, nt = 1;          // special rows: head 0..nh-1, tail n-nt..n-1
   DW hd[2][3];                 // head rows (a, b, c), double-word
@@ -74,26 +74,42 @@ __device__ __forceinline__ int tile_off(int r) {
   return (r / M) * (M + 1) + (r % M);
 }
 
-// FP32 chunked LU solve, in place on v (RHS in, solution out); t is scratch.
+// Per-row FP32 tables of one lane's chunk (padded chunk layout, see tile_off):
+//   l            forward multiplier l_i
+//   gwp = (g, w, phi, 0)  g_i = 1/u_i, w_i = c_i/u_i, phi_i = prod_{chunk start..i} (-l)
+//   psi          prod_{i..chunk end} (-w)
+// phi and psi are the responses of a chunk's local sweeps to the carry that
+// enters it; they depend only on the row position, so they are tabulated
+// once per plan instead of being recomputed (and held in registers) per row.
+struct ChunkTabs {
+  const float* l;
+  const float4* gwp;
+  const float* psi;
+};
+
+// The table loads of a fully unrolled sweep would otherwise all be hoisted
+// to its start (16 rows x up to 4 floats of live registers); a compiler-only
+// fence every 4 rows bounds how far ahead they are issued.
+#define NTK_TABLE_FENCE(k) \
+  if (((k) & 3) == 3) asm volatile("" ::: "memory")
+
+// FP32 chunked LU solve, in place on v (RHS in, solution out).
 // DECAY: the factor products over every chunk (prod |l|, prod |w| over M
 // rows) are below 2^-26, i.e. below FP32 rounding, so the carry entering a
 // chunk is the previous chunk's local end value alone and the carry scans
 // reduce to one shuffle each (the plan checks the products on the host).
 template <int M, bool DECAY>
-__device__ __forceinline__ void chunk_solve(float (&v)[M], float (&t)[M], const float* tl, const float* tg,
-                                            const float* tw, unsigned lane) {
-  float yh = 0.f, phi = 1.f;
+__device__ __forceinline__ void chunk_solve(float (&v)[M], const ChunkTabs& t, unsigned lane) {
+  float yh = 0.f;
 #pragma unroll
   for (int k = 0; k < M; ++k) {
-    const float l = tl[k];
-    yh = fmaf(-l, yh, v[k]);
-    phi = -l * phi;
+    yh = fmaf(-t.l[k], yh, v[k]);
     v[k] = yh;
-    t[k] = phi;
+    NTK_TABLE_FENCE(k);
   }
   float B = yh;
   if (!DECAY) {
-    float A = phi;
+    float A = t.gwp[M - 1].z;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const float Ap = __shfl_up_sync(FULL, A, d);
@@ -106,19 +122,18 @@ __device__ __forceinline__ void chunk_solve(float (&v)[M], float (&t)[M], const 
   }
   float Yprev = __shfl_up_sync(FULL, B, 1);
   if (lane == 0) Yprev = 0.f;
-  float xh = 0.f, psi = 1.f;
+  float xh = 0.f;
 #pragma unroll
   for (int k = M - 1; k >= 0; --k) {
-    const float y = fmaf(t[k], Yprev, v[k]);
-    const float w = tw[k];
-    xh = fmaf(-w, xh, tg[k] * y);
-    psi = -w * psi;
+    const float4 q = t.gwp[k];
+    const float y = fmaf(q.z, Yprev, v[k]);
+    xh = fmaf(-q.y, xh, q.x * y);
     v[k] = xh;
-    t[k] = psi;
+    NTK_TABLE_FENCE(k);
   }
   float B2 = xh;
   if (!DECAY) {
-    float A2 = psi;
+    float A2 = t.psi[0];
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const float Ap = __shfl_down_sync(FULL, A2, d);
@@ -132,7 +147,10 @@ __device__ __forceinline__ void chunk_solve(float (&v)[M], float (&t)[M], const 
   float Xnext = __shfl_down_sync(FULL, B2, 1);
   if (lane == 31) Xnext = 0.f;
 #pragma unroll
-  for (int k = 0; k < M; ++k) v[k] = fmaf(t[k], Xnext, v[k]);
+  for (int k = 0; k < M; ++k) {
+    v[k] = fmaf(t.psi[k], Xnext, v[k]);
+    NTK_TABLE_FENCE(k);
+  }
 }
 
 // r = D - A*x for one interior row, x = xh (+ xl).  A*xh is formed as an
@@ -174,44 +192,77 @@ struct RefineOcc {
   static constexpr int value = (M <= 16) ? NTK_REFINE_OCC : 1;
 };
 
+// Shared-memory footprint of one CTA: W padded system tiles plus the tables
+// (l and psi: 2 floats, gwp: a float4, per padded row).
+template <int M>
+__host__ __device__ constexpr size_t refine_smem(int W) {
+  return (size_t)W * sys_pitch<M>() * sizeof(double) + (size_t)32 * (M + 1) * (2 * sizeof(float) + sizeof(float4));
+}
+
+// x = s * (h + l) rounded to FP64 and stored (FP64 pipe: one DADD)
+__device__ __forceinline__ double scaled_out(float h, float l, const RefineArgs& ra) {
+  if (!ra.unit_scale) {
+    float p, e, oh, ol;
+    two_prod(ra.s.h, h, p, e);
+    e = fmaf(ra.s.h, l, e);
+    e = fmaf(ra.s.l, h, e);
+    fast_two_sum(p, e, oh, ol);
+    return dw_to_f64(oh, ol);
+  }
+  return dw_to_f64(h, l);
+}
+
 template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY>
 __global__ void __launch_bounds__(256, RefineOcc<M>::value)
     refine_kernel(const double* in, double* out, int n, Batch b, RefineArgs ra) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int P = sys_pitch<M>();
-  constexpr int NP = 32 * M;
+  constexpr int TS = 32 * (M + 1);  // table entries
   const int W = blockDim.x >> 5;
   double* tile = reinterpret_cast<double*>(smem_raw);
-  float* tab = reinterpret_cast<float*>(tile + (size_t)W * P);
+  float4* tgwp = reinterpret_cast<float4*>(tile + (size_t)W * P);  // 16-byte aligned: W*P*8 = W*(32(M+1)+1)*8
+  float* tl_all = reinterpret_cast<float*>(tgwp + TS);
+  float* tpsi_all = tl_all + TS;
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const unsigned lane = tid & 31;
   const long long s0 = (long long)blockIdx.x * W;
   const int wcount = (int)((b.nsys - s0) < W ? (b.nsys - s0) : W);
 
-  for (int i = tid; i < 3 * 32 * (M + 1); i += blockDim.x) tab[i] = ra.tab[i];
+  // tables: ra.tab holds [gwp (4 floats) | l | psi] per padded row
+  {
+    const float4* g4 = reinterpret_cast<const float4*>(ra.tab);
+    for (int i = tid; i < TS; i += blockDim.x) tgwp[i] = g4[i];
+    const float* lp = ra.tab + 4 * TS;
+    for (int i = tid; i < 2 * TS; i += blockDim.x) tl_all[i] = lp[i];
+  }
 
   // ---- stage the W systems: coalesced cp.async, all copies in flight at once ----
+  // Every thread copies M rows; the row of its q-th copy is lane + 32q (x:
+  // one system per warp) or tid / W + 32q (strided: blockDim / W == 32).
   if (b.es == 1) {
-    for (int w = warp; w < wcount; w += W) {
-      const long long s = s0 + w;
+    if (warp < wcount) {
+      const long long s = s0 + warp;
       const double* src = in + (s / b.ni) * b.os + (s % b.ni) * b.is;
-      double* trow = tile + (size_t)w * P;
-#pragma unroll 4
-      for (int r = lane; r < NP; r += 32) cp_async8(trow + tile_off<M>(r), src + (r < n ? r : 0), r < n ? 8u : 0u);
+      double* trow = tile + (size_t)warp * P;
+#pragma unroll
+      for (int q = 0; q < M; ++q) {
+        const int r = (int)lane + 32 * q;
+        cp_async8(trow + tile_off<M>(r), src + (r < n ? r : 0), r < n ? 8u : 0u);
+      }
     }
   } else {
-    // thread -> fixed system w = tid % W and every (blockDim / W)-th row: a
-    // warp reads 32 / W rows of W adjacent systems per instruction
     const int w = tid % W;
-    const int rstep = blockDim.x / W;
     if (w < wcount) {
       const long long s = s0 + w;
       const double* src = in + (s / b.ni) * b.os + (s % b.ni) * b.is;
       double* trow = tile + (size_t)w * P;
-#pragma unroll 4
-      for (int r = tid / W; r < NP; r += rstep)
+      const int rb = tid / W;
+#pragma unroll
+      for (int q = 0; q < M; ++q) {
+        const int r = rb + 32 * q;
         cp_async8(trow + tile_off<M>(r), src + (long long)(r < n ? r : 0) * b.es, r < n ? 8u : 0u);
+      }
     }
   }
   cp_async_wait_all();
@@ -223,9 +274,10 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
     const int r0 = j * M;
     const int cb = j * (M + 1);  // this lane's chunk in the tile
     float2* drow = reinterpret_cast<float2*>(trow);
-    const float* tl = tab + 0 * 32 * (M + 1) + cb;
-    const float* tg = tab + 1 * 32 * (M + 1) + cb;
-    const float* tw = tab + 2 * 32 * (M + 1) + cb;
+    ChunkTabs tabs;
+    tabs.l = tl_all + cb;
+    tabs.gwp = tgwp + cb;
+    tabs.psi = tpsi_all + cb;
     const int n1 = n - 1;
     const bool tail_here = (r0 <= n1) && (n1 < r0 + M);  // owns row n-1
     unsigned range = 0;
@@ -293,13 +345,16 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
     }
 
     // ---- FP32 solve ----
-    float tmp[M];
-    chunk_solve<M, DECAY>(x, tmp, tl, tg, tw, lane);
+    chunk_solve<M, DECAY>(x, tabs, lane);
 
-    // ---- refinement sweeps ----
+    // ---- refinement sweeps; the last one writes the FP64 result ----
     float xl[M];
 #pragma unroll
     for (int k = 0; k < M; ++k) xl[k] = 0.f;
+    if (SWEEPS == 0) {
+#pragma unroll
+      for (int k = 0; k < M; ++k) trow[cb + k] = scaled_out(x[k], 0.f, ra);
+    }
 #pragma unroll
     for (int sweep = 0; sweep < SWEEPS; ++sweep) {
       // every lane executes every shuffle (full mask); edges are zeroed after
@@ -407,17 +462,9 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
           }
         }
       }
-      chunk_solve<M, DECAY>(r, tmp, tl, tg, tw, lane);
-      if (sweep == 0) {
-        // x + delta exactly as a normalised double-word
-#pragma unroll
-        for (int k = 0; k < M; ++k) {
-          float h, e;
-          two_sum(x[k], r[k], h, e);
-          x[k] = h;
-          xl[k] = e;
-        }
-      } else {
+      chunk_solve<M, DECAY>(r, tabs, lane);
+      if (sweep + 1 < SWEEPS) {
+        // x + delta as a normalised double-word for the next sweep
 #pragma unroll
         for (int k = 0; k < M; ++k) {
           float h, e;
@@ -425,21 +472,19 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
           e += xl[k];
           fast_two_sum(h, e, x[k], xl[k]);
         }
-      }
-    }
-
-    // ---- FP64 output: x = s * xi ----
+      } else {
+        // last sweep: x + delta straight to the FP64 output slot
 #pragma unroll
-    for (int k = 0; k < M; ++k) {
-      float oh = x[k], ol = xl[k];
-      if (!ra.unit_scale) {
-        float p, e;
-        two_prod(ra.s.h, oh, p, e);
-        e = fmaf(ra.s.h, ol, e);
-        e = fmaf(ra.s.l, oh, e);
-        fast_two_sum(p, e, oh, ol);
+        for (int k = 0; k < M; ++k) {
+          float h, e;
+          two_sum(x[k], r[k], h, e);
+          if (sweep > 0) {
+            e += xl[k];
+            fast_two_sum(h, e, h, e);
+          }
+          trow[cb + k] = scaled_out(h, e, ra);
+        }
       }
-      trow[cb + k] = dw_to_f64(oh, ol);
     }
     if (range && ra.status) atomicOr(ra.status, 1u);
   }
@@ -447,39 +492,35 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
 
   // ---- store ----
   if (b.es == 1) {
-    for (int w = warp; w < wcount; w += W) {
-      const long long s = s0 + w;
+    if (warp < wcount) {
+      const long long s = s0 + warp;
       double* dst = out + (s / b.ni) * b.os + (s % b.ni) * b.is;
-      const double* trow = tile + (size_t)w * P;
-      if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
-#pragma unroll 4
-        for (int r = 2 * lane; r < n; r += 64) {
-          if (r + 1 < n)
-            *reinterpret_cast<double2*>(dst + r) = make_double2(trow[tile_off<M>(r)], trow[tile_off<M>(r + 1)]);
-          else
-            dst[r] = trow[tile_off<M>(r)];
-        }
-      } else {
-#pragma unroll 4
-        for (int r = lane; r < n; r += 32) dst[r] = trow[tile_off<M>(r)];
+      const double* trow = tile + (size_t)warp * P;
+#pragma unroll
+      for (int q = 0; q < M; ++q) {
+        const int r = (int)lane + 32 * q;
+        if (r < n) dst[r] = trow[tile_off<M>(r)];
       }
     }
   } else {
     const int w = tid % W;
-    const int rstep = blockDim.x / W;
     if (w < wcount) {
       const long long s = s0 + w;
       double* dst = out + (s / b.ni) * b.os + (s % b.ni) * b.is;
       const double* trow = tile + (size_t)w * P;
-#pragma unroll 4
-      for (int r = tid / W; r < n; r += rstep) dst[(long long)r * b.es] = trow[tile_off<M>(r)];
+      const int rb = tid / W;
+#pragma unroll
+      for (int q = 0; q < M; ++q) {
+        const int r = rb + 32 * q;
+        if (r < n) dst[(long long)r * b.es] = trow[tile_off<M>(r)];
+      }
     }
   }
 }
 
 template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY>
 int launch_one(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, int W, cudaStream_t st) {
-  const size_t smem = (size_t)W * sys_pitch<M>() * sizeof(double) + 3 * 32 * (M + 1) * sizeof(float);
+  const size_t smem = refine_smem<M>(W);
   auto kern = refine_kernel<M, RHS, SWEEPS, POW2, PAD, DECAY>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(refine_kernel)");
