@@ -149,6 +149,23 @@ int ntk_adi_step(ntk_adi* adi, double* u, double* d_x, const double* d_y, void* 
  * (u, d_x, d_y, steps) into a CUDA graph and replays it on later calls. */
 int ntk_adi_run(ntk_adi* adi, double* u, double* d_x, const double* d_y, int steps, int use_graph, void* stream);
 
+/* ---- ADI step that allocates nothing ----------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory (code running against a fixed, pre-sized memory budget, hosts with
+ * no device allocator, libraries that may only touch the buffers they are
+ * given): the same
+ * step as ntk_adi_step without a plan, with its work array and factor tables
+ * in one static device array of NTK_ADI_STATIC_MAX_N^2 + 3 NTK_ADI_STATIC_MAX_N
+ * doubles (~2 MiB, held by every GPU that loads the library until exit).
+ * N above NTK_ADI_STATIC_MAX_N is rejected with NTK_ERR_INVALID.  Calls no
+ * cudaMalloc/cudaFree.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make it before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race.  The factor
+ * tables are copied in on `stream` by every call (cudaMemcpyAsync from a
+ * per-thread host buffer). */
+#define NTK_ADI_STATIC_MAX_N 512
+int ntk_adi_step_static(int N, double dx, double dt, double* u, double* d_x, const double* d_y, void* stream);
+
 /* ---- uneven batches ------------------------------------------------------
  * nsys independent near-Toeplitz systems of different lengths and
  * coefficients in one buffer, solved in place by one persistent launch.

@@ -1,0 +1,187 @@
+// ntk_adi_static.cu -- an ADI time step that allocates nothing.
+//
+// ntk_adi_create/ntk_adi_step allocate device memory (factor tables and an
+// N x N work array for the segmented sweeps) when the plan is built.  Some
+// callers cannot do that: code that runs against a fixed, pre-sized memory
+// budget that must not grow, hosts with no device allocator, and libraries
+// that are handed only the user's buffers and are not allowed to call
+// cudaMalloc/cudaFree behind the caller's back.  For them,
+// ntk_adi_step_static performs the same step as ntk_adi_step but keeps its
+// work array and factor tables in one file-scope __device__ array of fixed
+// size, NTK_ADI_STATIC_MAX_N^2 + 3 * NTK_ADI_STATIC_MAX_N doubles (about
+// 2 MiB), which every GPU that loads the library holds until the process
+// exits.
+//
+// The array is shared by every call: calls that overlap on the GPU (for
+// example on two streams, or from two host threads) race on it.  It keeps the
+// last call's contents; the factor tables are re-uploaded by every call and
+// every entry of the work array that a call reads is written earlier in the
+// same call, so nothing needs clearing.
+//
+// In host code the array's name is only a host-side stand-in, not a device
+// address, so the device address is looked up with cudaGetSymbolAddress, once
+// per device, by the first call made with that device current.  That first
+// call should come before any stream capture on the device.
+#include <cmath>
+#include <mutex>
+
+#include "ntk_internal.h"
+
+namespace ntk {
+namespace {
+
+constexpr int kMaxN = NTK_ADI_STATIC_MAX_N;
+constexpr int kMaxDevices = 64;
+
+// [0, N*N): work array of the segmented sweeps; then l[N], w[N], g[N]
+__device__ __align__(256) double g_adi_static_scratch[(size_t)kMaxN * kMaxN + 3 * kMaxN];
+
+double* g_scratch_addr[kMaxDevices] = {nullptr};
+std::mutex g_scratch_mu;
+
+int scratch_address(int dev, double** out) {
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    int rc = cuda_status(cudaGetSymbolAddress(&p, g_adi_static_scratch), "cudaGetSymbolAddress(ADI scratch)");
+    if (rc) return rc;
+    g_scratch_addr[dev] = static_cast<double*>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return NTK_OK;
+}
+
+// Same rule as the ADI plan: smallest halo whose windows' factor products
+// are below 2^-64, enough segments to cover the GPU; plain sweeps otherwise.
+SegParams static_segments(const double* l, const double* w, int n, long long nsys) {
+  SegParams sp;
+  sp.P = 1;
+  sp.L = n;
+  sp.H = 0;
+  int P = 1;
+  while (nsys * P < 152LL * 96 && P < 64 && n / (2 * P) >= 64) P *= 2;
+  if (P == 1) return sp;
+  const int L = (n + P - 1) / P;
+  const double lim = std::ldexp(1.0, -64);
+  for (int H = 8; H <= L / 2; H += 2) {
+    bool ok = true;
+    for (int g = 1; g < P && ok; ++g) {
+      double prod = 1.0;
+      for (int i = (g * L - H > 1 ? g * L - H : 1); i < g * L; ++i) prod *= std::fabs(l[i]);
+      ok = prod <= lim;
+    }
+    for (int g = 0; g < P - 1 && ok; ++g) {
+      double prod = 1.0;
+      const int e = ((g + 1) * L < n) ? (g + 1) * L : n;
+      for (int i = e; i < ((e + H < n) ? e + H : n); ++i) prod *= std::fabs(w[i - 1]);
+      ok = prod <= lim;
+    }
+    if (ok) {
+      sp.P = P;
+      sp.L = L;
+      sp.H = H;
+      return sp;
+    }
+  }
+  return sp;
+}
+
+}  // namespace
+}  // namespace ntk
+
+extern "C" int ntk_adi_step_static(int N, double dx, double dt, double* u, double* d_x, const double* d_y,
+                                   void* stream) {
+  using namespace ntk;
+  if (!u || !d_x || !d_y) {
+    set_error("ntk_adi_step_static: null array");
+    return NTK_ERR_INVALID;
+  }
+  if (N < 4 || N > kMaxN) {
+    set_error("ntk_adi_step_static: N = %d outside 4..%d (the static work array holds N <= %d)", N, kMaxN, kMaxN);
+    return NTK_ERR_INVALID;
+  }
+  if (!(dx > 0) || !(dt > 0) || !std::isfinite(dx) || !std::isfinite(dt)) {
+    set_error("ntk_adi_step_static: need positive finite dx, dt");
+    return NTK_ERR_INVALID;
+  }
+  int dev = -1;
+  int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc) return rc;
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error("ntk_adi_step_static: device ordinal %d not supported", dev);
+    return NTK_ERR_UNSUPPORTED;
+  }
+  double* scratch = nullptr;
+  if ((rc = scratch_address(dev, &scratch))) return rc;
+
+  // Factor tables of experiments/run-adi.py:50-53's matrix, built on the host
+  // in a fixed per-thread buffer (no allocation): l, w, g with g = 1/u.
+  static thread_local double tabs[3 * kMaxN];
+  double* l = tabs;
+  double* w = tabs + N;
+  double* g = tabs + 2 * N;
+  const double a_in = 1. / (dx * dx), b_in = -2. * (1. / dt + 1. / (dx * dx)), c_in = 1. / (dx * dx);
+  // rows: 0 = (1, 0), interior = (a_in, b_in, c_in), N-1 = (0, 1)
+  double u_prev = 1.0;
+  l[0] = 0.0;
+  for (int i = 0; i < N; ++i) {
+    const double ai = (i == 0 || i == N - 1) ? 0.0 : a_in;
+    const double bi = (i == 0 || i == N - 1) ? 1.0 : b_in;
+    const double ci_prev = (i - 1 == 0) ? 0.0 : c_in;  // c of row i-1 (row 0 has c = 0)
+    double ui = bi;
+    if (i > 0) {
+      l[i] = ai / u_prev;
+      ui = bi - l[i] * ci_prev;
+    }
+    if (!(ui != 0.0) || !std::isfinite(ui)) {
+      set_error("ntk_adi_step_static: zero or non-finite pivot");
+      return NTK_ERR_INVALID;
+    }
+    const double ci = (i == 0 || i == N - 1) ? 0.0 : c_in;
+    w[i] = ci / ui;
+    g[i] = 1.0 / ui;
+    u_prev = ui;
+  }
+  const SegParams sp = static_segments(l, w, N, N - 2);
+
+  cudaStream_t st = (cudaStream_t)stream;
+  double* dtab = scratch + (size_t)kMaxN * kMaxN;
+  rc = cuda_status(cudaMemcpyAsync(dtab, tabs, sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice, st),
+                   "cudaMemcpyAsync(ADI static tables)");
+  if (rc) return rc;
+  TablesF64 t;
+  t.l = dtab;
+  t.w = dtab + N;
+  t.g = dtab + 2 * N;
+  const double bottom = -1. / (dx * dx), top = -1. / (dx * dx), center = 2 * (-1. / dt + 1. / (dx * dx));
+  // x half step (rows 1..N-2 of d_x), then y half step (columns 1..N-2, into u)
+  Batch bx;
+  bx.nsys = N - 2;
+  bx.ni = N - 2;
+  bx.is = N;
+  bx.os = 0;
+  bx.es = 1;
+  RhsParams rx;
+  rx.kind = RHS_CROSS;
+  rx.bottom = bottom;
+  rx.center = center;
+  rx.top = top;
+  rx.cs = N;
+  rx.bnd = d_x + N;
+  rx.bnd_ss = N;
+  rx.bnd_es = 1;
+  rc = launch_thomas_f64_segmented(u + N, scratch + N, d_x + N, N, bx, rx, t, sp, st);
+  if (rc) return rc;
+  Batch by;
+  by.nsys = N - 2;
+  by.ni = N - 2;
+  by.is = 1;
+  by.os = 0;
+  by.es = N;
+  RhsParams ry = rx;
+  ry.cs = 1;
+  ry.bnd = d_y + N;
+  ry.bnd_ss = N;
+  ry.bnd_es = 1;
+  return launch_thomas_f64_segmented(d_x + 1, scratch + 1, u + 1, N, by, ry, t, sp, st);
+}

@@ -54,6 +54,7 @@ SIGNATURES = [
     ("ntk_adi_segments", _i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     ("ntk_adi_step", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("ntk_adi_run", _i, [_vp, _vp, _vp, _vp, _i, _i, _vp]),
+    ("ntk_adi_step_static", _i, [_i, _d, _d, _vp, _vp, _vp, _vp]),
     ("ntk_batch_create", _i, [ctypes.POINTER(_vp), _ll, _vp, _vp, _vp, _vp, _vp, _i]),
     ("ntk_batch_destroy", _i, [_vp]),
     ("ntk_batch_info", _i, [_vp, ctypes.POINTER(_ll), ctypes.POINTER(_ll), ctypes.POINTER(_ll)]),
