@@ -8,8 +8,8 @@
 // out of its inner loops: FP64 inputs are split into two floats with
 // integer operations, the residual is formed with error-free
 // transformations (TwoSum / TwoProd, Knuth 1969, Dekker 1971; accurate
-// summation after Ogita, Rump and Oishi 2005), and a single DADD per row
-// rebuilds the FP64 output.
+// summation after Ogita, Rump and Oishi 2005), and the FP64 output is
+// assembled from the double-word with integer operations.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -61,24 +61,29 @@ __device__ __forceinline__ void split_f64(double x, float& hi, float& lo, unsign
   range_flag |= (mag >= (1151u << 20)) ? 1u : 0u;
 }
 
-// float -> double by bit manipulation (normal floats and zero; denormals
-// flush to zero).
-__device__ __forceinline__ double f32_to_f64_bits(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned m = b & 0x7fffffffu;
-  unsigned hi = (m >> 3) + (896u << 20);
-  hi = (m >= 0x00800000u) ? hi : 0u;
-  const unsigned lo = (m >= 0x00800000u) ? (b << 29) : 0u;
-  return __hiloint2double((int)(hi | (b & 0x80000000u)), (int)lo);
-}
-
-// hi + lo (a normalised double-word) rounded to the nearest double
+// hi + lo (a normalised double-word: |lo| <= ulp(hi)/2) as a double, with
+// INT and FP32 operations only (no DADD on the slow FP64 pipe).  lo is
+// expressed in units of 64 ulps of hi-as-a-double: lo * 2^(46 - e_hi) lies
+// within +-2^22, so adding 1.5 * 2^23 rounds it to an integer k held in the
+// float's low mantissa bits, and k * 64 is added to the 64-bit pattern of
+// hi.  hi's low 29 mantissa bits are zero and |64 k| <= 2^28, so the sum
+// never crosses a binade, except below an exact power of two (hi = +-2^e
+// and lo of the other sign), where the double's ulp halves and k is doubled.
+// Relative error <= 2^-47, the precision the double-word carries; |hi| below
+// 2^-81 (and zero) gives zero.
 __device__ __forceinline__ double dw_to_f64(float hi, float lo) {
-#ifdef NTK_F2D_HW
-  return (double)hi + (double)lo;
-#else
-  return f32_to_f64_bits(hi) + f32_to_f64_bits(lo);
-#endif
+  const unsigned bh = __float_as_uint(hi);
+  const unsigned eh = bh & 0x7f800000u;
+  // 2^(46 - e_hi) carrying hi's sign: k > 0 moves away from zero
+  const float sc = __uint_as_float(((300u << 23) - eh) | (bh & 0x80000000u));
+  const float t = __fadd_rn(__fmul_rn(lo, sc), 12582912.0f);
+  int k = (int)(__float_as_uint(t) - 0x4b400000u);
+  if ((bh & 0x007fffffu) == 0u && k < 0) k *= 2;
+  const unsigned dhi = ((bh & 0x7fffffffu) >> 3) + (896u << 20);
+  const unsigned dlo = bh << 29;
+  unsigned long long bits = (((unsigned long long)dhi << 32) | dlo) + (unsigned long long)((long long)k << 6);
+  bits = (eh >= (46u << 23)) ? bits : 0ull;
+  return __longlong_as_double((long long)(bits | ((unsigned long long)(bh & 0x80000000u) << 32)));
 }
 
 // ---------------------------------------------------------------------------

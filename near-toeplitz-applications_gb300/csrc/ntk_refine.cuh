@@ -8,14 +8,17 @@
 // per row, ~1.45 rows per clock per SM.  The FP64 pipe retires ~1.7
 // instructions per clock per SM, so the plain FP64 solve (4 FP64
 // instructions per row) tops out near 30% of HBM.  Here the FP64 pipe is used
-// once per row (the DADD that assembles the FP64 output) and everything else
-// runs on the FP32/INT pipes:
-//   * the FP64 input is split into a float pair with integer operations;
-//   * the RHS difference, the residual r = d - A x and the accumulation of the
-//     correction use error-free transformations (TwoSum/TwoProd), so they
-//     carry ~48 significant bits -- what an FP64 residual would supply for a
-//     1e-12 result (the FP32 solve leaves ~5e-7, one sweep ~(5e-7)^2 * cond);
-//   * the FP32 solves run on register-resident chunks.
+// once per row (the DADD that forms the compact RHS difference f_{i+1} -
+// f_{i-1} exactly as the FP64 path does) and everything else runs on the
+// FP32/INT pipes:
+//   * the FP64 difference is split into a float pair with integer operations;
+//   * the residual r = d - A x and the accumulation of the correction use
+//     error-free transformations (TwoSum/TwoProd), so they carry ~48
+//     significant bits -- what an FP64 residual would supply for a 1e-12
+//     result (the FP32 solve leaves ~5e-7, one sweep ~(5e-7)^2 * cond);
+//   * the FP32 solves run on register-resident chunks;
+//   * the FP64 output is assembled from the double-word with integer
+//     operations (dw_to_f64).
 //
 // Work decomposition.  A CTA stages W systems into shared memory with
 // coalesced loads (contiguous systems: lanes walk rows; strided y/z systems:
@@ -192,14 +195,28 @@ struct RefineOcc {
   static constexpr int value = (M <= 16) ? NTK_REFINE_OCC : 1;
 };
 
-// Shared-memory footprint of one CTA: W padded system tiles plus the tables
-// (l and psi: 2 floats, gwp: a float4, per padded row).
+// Shared-memory footprint of one CTA: W padded system tiles, the tables
+// (l and psi: 2 floats, gwp: a float4, per padded row) and the double-word
+// boundary right-hand sides (rows 0 and n-1 of each system).
 template <int M>
 __host__ __device__ constexpr size_t refine_smem(int W) {
-  return (size_t)W * sys_pitch<M>() * sizeof(double) + (size_t)32 * (M + 1) * (2 * sizeof(float) + sizeof(float4));
+  return (size_t)W * sys_pitch<M>() * sizeof(double) + (size_t)32 * (M + 1) * (2 * sizeof(float) + sizeof(float4)) +
+         (size_t)2 * W * sizeof(float2);
 }
 
-// x = s * (h + l) rounded to FP64 and stored (FP64 pipe: one DADD)
+// Offset of system s's first unknown: (s / ni) * os + (s % ni) * is, with
+// 32-bit division whenever the operands allow.
+__device__ __forceinline__ long long sys_offset(long long s, const Batch& b) {
+  if (b.ni >= b.nsys) return s * b.is;
+  if (s <= 0x7fffffffLL && b.ni <= 0x7fffffffLL) {
+    const unsigned q = (unsigned)s / (unsigned)b.ni;
+    const unsigned r = (unsigned)s - q * (unsigned)b.ni;
+    return (long long)q * b.os + (long long)r * b.is;
+  }
+  return (s / b.ni) * b.os + (s % b.ni) * b.is;
+}
+
+// x = s * (h + l) as an FP64 value (no FP64 instruction)
 __device__ __forceinline__ double scaled_out(float h, float l, const RefineArgs& ra) {
   if (!ra.unit_scale) {
     float p, e, oh, ol;
@@ -217,17 +234,20 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
     refine_kernel(const double* in, double* out, int n, Batch b, RefineArgs ra) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int P = sys_pitch<M>();
-  constexpr int TS = 32 * (M + 1);  // table entries
+  constexpr int TS = 32 * (M + 1);        // table entries
+  constexpr int QSTEP = (32 / M) * (M + 1);  // tile_off(r + 32) - tile_off(r)
   const int W = blockDim.x >> 5;
   double* tile = reinterpret_cast<double*>(smem_raw);
   float4* tgwp = reinterpret_cast<float4*>(tile + (size_t)W * P);  // 16-byte aligned: W*P*8 = W*(32(M+1)+1)*8
   float* tl_all = reinterpret_cast<float*>(tgwp + TS);
   float* tpsi_all = tl_all + TS;
+  float2* bnd = reinterpret_cast<float2*>(tpsi_all + TS);  // [2 * W]: rows 0 and n-1
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const unsigned lane = tid & 31;
   const long long s0 = (long long)blockIdx.x * W;
   const int wcount = (int)((b.nsys - s0) < W ? (b.nsys - s0) : W);
+  unsigned range = 0;
 
   // tables: ra.tab holds [gwp (4 floats) | l | psi] per padded row
   {
@@ -238,31 +258,40 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
   }
 
   // ---- stage the W systems: coalesced cp.async, all copies in flight at once ----
-  // Every thread copies M rows; the row of its q-th copy is lane + 32q (x:
-  // one system per warp) or tid / W + 32q (strided: blockDim / W == 32).
-  if (b.es == 1) {
-    if (warp < wcount) {
-      const long long s = s0 + warp;
-      const double* src = in + (s / b.ni) * b.os + (s % b.ni) * b.is;
-      double* trow = tile + (size_t)warp * P;
+  // Every thread copies M rows; the row of its q-th copy is rb + 32q, with
+  // rb = lane (x: one system per warp) or tid / W (strided: blockDim / W ==
+  // 32), so its tile slot is tile_off(rb) + q * QSTEP.  The same thread
+  // stores the same rows at the end.
+  const int sw = (b.es == 1) ? warp : tid % W;  // system (within the CTA) this thread copies
+  const int rb = (b.es == 1) ? (int)lane : tid / W;
+  if (sw < wcount) {
+    const double* gsrc = in + sys_offset(s0 + sw, b) + (long long)rb * b.es;
+    double* tslot = tile + (size_t)sw * P + tile_off<M>(rb);
+    const long long gstep = 32LL * b.es;
 #pragma unroll
-      for (int q = 0; q < M; ++q) {
-        const int r = (int)lane + 32 * q;
-        cp_async8(trow + tile_off<M>(r), src + (r < n ? r : 0), r < n ? 8u : 0u);
-      }
+    for (int q = 0; q < M; ++q) {
+      const bool ok = !PAD || rb + 32 * q < n;
+      cp_async8(tslot + q * QSTEP, ok ? gsrc + q * gstep : in, ok ? 8u : 0u);
     }
-  } else {
-    const int w = tid % W;
+  }
+  // The compact scheme's one-sided boundary stencils (compact/rhs.py:21-31)
+  // in FP64, for all W systems at once by the first warp (lane 2w: row 0 of
+  // system w, lane 2w+1: row n-1), read straight from global memory while the
+  // copies are in flight: one set of FP64 instructions per CTA instead of
+  // one per system.
+  if (RHS == RHS_COMPACT && warp == 0) {
+    const int w = (int)(lane >> 1);
     if (w < wcount) {
-      const long long s = s0 + w;
-      const double* src = in + (s / b.ni) * b.os + (s % b.ni) * b.is;
-      double* trow = tile + (size_t)w * P;
-      const int rb = tid / W;
-#pragma unroll
-      for (int q = 0; q < M; ++q) {
-        const int r = rb + 32 * q;
-        cp_async8(trow + tile_off<M>(r), src + (long long)(r < n ? r : 0) * b.es, r < n ? 8u : 0u);
-      }
+      const bool tl = lane & 1;
+      const double* f = in + sys_offset(s0 + w, b);
+      const long long e = b.es;
+      const long long q0 = tl ? (long long)(n - 1) * e : 0, q1 = tl ? (long long)(n - 2) * e : e,
+                      q2 = tl ? (long long)(n - 3) * e : 2 * e;
+      const double v = (tl ? ra.sigmaN : ra.sigma0) * ((-5.0 * __ldg(f + q0) + 4.0 * __ldg(f + q1)) + __ldg(f + q2));
+      float h, l;
+      split_f64(v, h, l, range);
+      fast_two_sum(h, l, h, l);
+      bnd[lane] = make_float2(h, l);
     }
   }
   cp_async_wait_all();
@@ -280,24 +309,14 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
     tabs.psi = tpsi_all + cb;
     const int n1 = n - 1;
     const bool tail_here = (r0 <= n1) && (n1 < r0 + M);  // owns row n-1
-    unsigned range = 0;
     float x[M];
 
     // ---- RHS in double-word, written back into the tile slots ----
     if (RHS == RHS_COMPACT) {
       // D_r = f_{r+1} - f_{r-1} is formed in FP64 (one DADD, as in the FP64
       // path) and then split: a double-word split of f itself keeps only
-      // ~2^-47 |f|, too coarse when f_{r+1} and f_{r-1} nearly cancel.
-      // One-sided boundary stencils (compact/rhs.py:21-31) in FP64, evaluated
-      // once per warp: lane 0 evaluates row 0, the lane owning row n-1 that
-      // row, the other lanes a discarded copy (a divergent evaluation would
-      // cost the slow FP64 pipe a full warp instruction per row).
-      const int q0 = tail_here ? n1 : 0, q1 = tail_here ? n1 - 1 : 1, q2 = tail_here ? n1 - 2 : 2;
-      const double dsp = (tail_here ? ra.sigmaN : ra.sigma0) *
-                         ((-5.0 * trow[tile_off<M>(q0)] + 4.0 * trow[tile_off<M>(q1)]) + trow[tile_off<M>(q2)]);
-      double dsp0 = dsp, dsp1 = dsp;
-      if (j == 0 && tail_here)  // only when one lane holds the whole system
-        dsp0 = ra.sigma0 * ((-5.0 * trow[tile_off<M>(0)] + 4.0 * trow[tile_off<M>(1)]) + trow[tile_off<M>(2)]);
+      // ~2^-47 |f|, too coarse when f_{r+1} and f_{r-1} nearly cancel.  Rows 0
+      // and n-1 take the boundary stencils staged in bnd.
       const double fleft = (j > 0) ? trow[tile_off<M>(r0 - 1)] : 0.0;
       const double fright = (j < 31) ? trow[tile_off<M>(r0 + M)] : 0.0;
       __syncwarp();  // the neighbours' halo reads happen before any slot is rewritten
@@ -314,16 +333,13 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
         fcur = fnext;
       }
       if (j == 0) {
-        float h, l;
-        split_f64(dsp0, h, l, range);
-        fast_two_sum(h, l, h, l);
-        x[0] = h;
-        drow[cb + 0] = make_float2(h, l);
+        const float2 d0 = bnd[2 * warp];
+        x[0] = d0.x;
+        drow[cb + 0] = d0;
       }
       if (tail_here) {
-        float h, l;
-        split_f64(dsp1, h, l, range);
-        fast_two_sum(h, l, h, l);
+        const float2 d1 = bnd[2 * warp + 1];
+        const float h = d1.x;
         if (!PAD) {
           x[M - 1] = h;
         } else {
@@ -331,7 +347,7 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
           for (int k = 0; k < M; ++k)
             if (r0 + k == n1) x[k] = h;
         }
-        drow[tile_off<M>(n1)] = make_float2(h, l);
+        drow[tile_off<M>(n1)] = d1;
       }
     } else {
 #pragma unroll
@@ -486,35 +502,18 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
         }
       }
     }
-    if (range && ra.status) atomicOr(ra.status, 1u);
   }
+  if (range && ra.status) atomicOr(ra.status, 1u);
   __syncthreads();
 
-  // ---- store ----
-  if (b.es == 1) {
-    if (warp < wcount) {
-      const long long s = s0 + warp;
-      double* dst = out + (s / b.ni) * b.os + (s % b.ni) * b.is;
-      const double* trow = tile + (size_t)warp * P;
+  // ---- store: each thread writes back the rows it staged ----
+  if (sw < wcount) {
+    double* gdst = out + sys_offset(s0 + sw, b) + (long long)rb * b.es;
+    const double* tslot = tile + (size_t)sw * P + tile_off<M>(rb);
+    const long long gstep = 32LL * b.es;
 #pragma unroll
-      for (int q = 0; q < M; ++q) {
-        const int r = (int)lane + 32 * q;
-        if (r < n) dst[r] = trow[tile_off<M>(r)];
-      }
-    }
-  } else {
-    const int w = tid % W;
-    if (w < wcount) {
-      const long long s = s0 + w;
-      double* dst = out + (s / b.ni) * b.os + (s % b.ni) * b.is;
-      const double* trow = tile + (size_t)w * P;
-      const int rb = tid / W;
-#pragma unroll
-      for (int q = 0; q < M; ++q) {
-        const int r = rb + 32 * q;
-        if (r < n) dst[(long long)r * b.es] = trow[tile_off<M>(r)];
-      }
-    }
+    for (int q = 0; q < M; ++q)
+      if (!PAD || rb + 32 * q < n) gdst[q * gstep] = tslot[q * QSTEP];
   }
 }
 

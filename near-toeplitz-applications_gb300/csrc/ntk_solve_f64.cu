@@ -403,35 +403,45 @@ __global__ void __launch_bounds__(32) thomas_f64_staged_kernel(const double* __r
 // in, x tiles out.  Needs es == 1 and the 32 systems of a warp to be
 // equally spaced (is), which the launcher checks.
 // ----------------------------------------------------------------------------
-constexpr int XT = 32;       // rows per tile
-constexpr int XP = XT + 1;   // tile pitch (doubles)
+constexpr int XT = 16;       // rows per tile
+constexpr int XP = 33;       // tile pitch (doubles): one row of the tile holds 32 systems + 1 pad
 constexpr int XRING = 3;     // tiles in flight per warp
 constexpr int XWARPS = 4;    // warps per CTA
+constexpr int XSUB = 32 / XT;  // systems covered by one warp instruction of the tile copies
 
+// tile[row][w] <- system w, global row row0 + row: lanes cover XT rows of
+// XSUB systems per instruction (coalesced XT*8-byte segments)
 __device__ __forceinline__ void xtile_issue(double* tile, const double* base0, long long is, int cnt, int row0, int n,
                                             int lane) {
-  const int r = row0 + lane;
+  const int k = lane % XT;
+  const int ws = lane / XT;
+  const int r = row0 + k;
   const bool ok = r < n;
 #pragma unroll 8
-  for (int w = 0; w < 32; ++w) {
+  for (int w0 = 0; w0 < 32; w0 += XSUB) {
+    const int w = w0 + ws;
     const bool v = ok && (w < cnt);
-    cp_async8(tile + lane * XP + w, base0 + (v ? (long long)w * is + r : 0), v ? 8u : 0u);
+    cp_async8(tile + k * XP + w, base0 + (v ? (long long)w * is + r : 0), v ? 8u : 0u);
   }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
 __device__ __forceinline__ void xtile_store(const double* tile, double* base0, long long is, int cnt, int row0, int n,
                                             int lane) {
-  const int r = row0 + lane;
+  const int k = lane % XT;
+  const int ws = lane / XT;
+  const int r = row0 + k;
   if (r < n) {
 #pragma unroll 8
-    for (int w = 0; w < 32; ++w)
-      if (w < cnt) base0[(long long)w * is + r] = tile[lane * XP + w];
+    for (int w0 = 0; w0 < 32; w0 += XSUB) {
+      const int w = w0 + ws;
+      if (w < cnt) base0[(long long)w * is + r] = tile[k * XP + w];
+    }
   }
 }
 
 template <int RHS>
-__global__ void __launch_bounds__(XT * XWARPS) thomas_f64_xpose_kernel(const double* in, double* out, int n, Batch b,
+__global__ void __launch_bounds__(32 * XWARPS) thomas_f64_xpose_kernel(const double* in, double* out, int n, Batch b,
                                                                        RhsParams rp, TablesF64 t) {
   extern __shared__ __align__(16) double xsm[];
   const int lane = threadIdx.x & 31;
@@ -567,11 +577,11 @@ int launch_thomas_f64(const double* in, double* out, int n, const Batch& b, cons
     if (rp.kind == RHS_IDENTITY) {
       auto k = thomas_f64_xpose_kernel<RHS_IDENTITY>;
       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs);
-      k<<<(unsigned)xblocks, XT * XWARPS, xs, stream>>>(in, out, n, b, rp, t);
+      k<<<(unsigned)xblocks, 32 * XWARPS, xs, stream>>>(in, out, n, b, rp, t);
     } else {
       auto k = thomas_f64_xpose_kernel<RHS_COMPACT>;
       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xs);
-      k<<<(unsigned)xblocks, XT * XWARPS, xs, stream>>>(in, out, n, b, rp, t);
+      k<<<(unsigned)xblocks, 32 * XWARPS, xs, stream>>>(in, out, n, b, rp, t);
     }
     return cuda_status(cudaGetLastError(), "thomas_f64_xpose_kernel");
   }
