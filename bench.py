@@ -403,6 +403,7 @@ def run_gpu(args):
                "sample": "%d system solves of n=512 (x, y, z lines of the 512^3 field), numpy RHS + scipy "
                          "solve_banded (experiments/run-compact.py:14-28), 1 process, %.1f s of CPU time"
                          % (rows // N, wall)}
+    extra = {} if args.no_secondary else secondary_configs(dev, hbm)
     line = {
         "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_main, "higher_is_better": True, "scaling": "weak",
@@ -432,10 +433,116 @@ def run_gpu(args):
         "gpu_launches": 3 * args.steps,
         "clocks": clocks.summary(),
     }
+    line.update(extra)
     print(json.dumps(line), flush=True)
     for p in plans.values():
         p.close()
     return 0
+
+
+def secondary_configs(dev, hbm):
+    """The other measured workloads (rank 0, FP64 path, outside the headline):
+    ADI 2048^2, r = 0.5, 100 steps replayed as one CUDA graph
+    (experiments/run-adi.py:59-71); the uneven batch of 4096 systems with
+    lengths log-uniform in [32, 8192] in one persistent launch.  Each with
+    rows/s, HBM fraction of its algorithmic bytes, error against the oracle
+    and the reference's CPU path timed on a bounded sample."""
+    import time
+
+    import numpy as np
+    import torch
+
+    import ntk
+    from ntk.workloads import gaussians_2d, uneven_batch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    res = {}
+    # ---- ADI ----
+    NA, steps = 2048, 100
+    dx = 1.0 / (NA - 1)
+    dt = 2 * 0.5 * dx * dx
+    u0 = gaussians_2d(NA, seed=0, device=dev)
+    u, dxa, dya = u0.clone(), u0.clone(), u0.t().contiguous()
+    with ntk.Adi(NA, dx, dt) as adi:
+        adi.run(u, dxa, dya, steps, graph=True)  # capture + warm
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        adi.run(u, dxa, dya, steps, graph=True)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        # accuracy: 3 steps from u0 against the long-double Thomas pipeline
+        ug, xg, yg = u0.clone(), u0.clone(), u0.t().contiguous()
+        for _ in range(3):
+            adi.step(ug, xg, yg)
+        torch.cuda.synchronize(dev)
+    ub = u0.cpu().numpy().copy()
+    xb, yb = ub.copy(), ub.T.copy()
+    for _ in range(3):
+        O.adi_step_exact(ub, xb, yb, dx, dt)
+    err = O.rel_err(ug.cpu().numpy(), ub)
+    uc = u0.cpu().numpy().copy()
+    xc, yc = uc.copy(), uc.T.copy()
+    t0 = time.perf_counter()
+    O.adi_step_banded(uc, xc, yc, dx, dt)
+    cpu_s = time.perf_counter() - t0
+    rows = 2 * (NA - 2) * NA
+    res["adi"] = {"workload": "ADI heat equation 2048^2, r = 0.5, %d steps as one CUDA graph" % steps,
+                  "precision": "fp64", "ms_per_step": ms, "rows_per_s": rows / (ms * 1e-3),
+                  "hbm_frac": 32.0 * NA * NA / (ms * 1e-3) / 1e9 / hbm,
+                  "rel_err_vs_oracle_3_steps": err,
+                  "cpu_baseline": {"rows_per_s": rows / cpu_s, "cores": 1, "kind": "port",
+                                   "sample": "one step, numpy stencil + scipy solve_banded per half step"}}
+    del u, dxa, dya, ug, xg, yg, u0
+    # ---- uneven batch ----
+    lengths, systems = uneven_batch(4096, 32, 8192, seed=0)
+    interior = np.array([sy[0] for sy in systems])
+    head = np.array([sy[1] for sy in systems])
+    tail = np.array([sy[2] for sy in systems])
+    with ntk.UnevenBatch(lengths, interior, head, tail) as bt:
+        total = bt.elements
+        offs = np.asarray(bt.offsets)
+        d = np.random.default_rng(1).normal(size=total)
+        t = torch.from_numpy(d).to(dev)
+        bt.solve(t)
+        torch.cuda.synchronize(dev)
+        x = t.cpu().numpy()
+        reps = 50
+        for _ in range(3):
+            bt.solve(t)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            bt.solve(t)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / reps
+    rng = np.random.default_rng(2)
+    worst = 0.0
+    cpu_rows = 0
+    t0 = time.perf_counter()
+    for s in rng.choice(len(lengths), size=128, replace=False):
+        n = int(lengths[s])
+        o = int(offs[s])
+        a, b, c = O.near_toeplitz_bands_general(n, interior[s], head[s], tail[s])
+        ref = O.tridiagonal_solve(a, b, c, d[o:o + n])
+        cpu_rows += n
+        worst = max(worst, O.rel_err(x[o:o + n], ref))
+    cpu_s = time.perf_counter() - t0
+    total_rows = int(np.sum(lengths))
+    res["uneven_batch"] = {"workload": "4096 systems, lengths log-uniform in [32, 8192], one persistent launch",
+                           "precision": "fp64", "rows": total_rows, "ms": ms, "rows_per_s": total_rows / (ms * 1e-3),
+                           "hbm_frac": 16.0 * total_rows / (ms * 1e-3) / 1e9 / hbm,
+                           "rel_err_vs_banded_oracle_128_systems": worst,
+                           "cpu_baseline": {"rows_per_s": cpu_rows / cpu_s, "cores": 1, "kind": "port",
+                                            "sample": "128 systems, one scipy solve_banded each"}}
+    return res
 
 
 def sample_oracle_errors(f, ref, h, lines=256):
@@ -499,6 +606,8 @@ def main():
     ap.add_argument("--precision", default="fp32_refine", choices=["fp64", "fp32", "fp32_refine"])
     ap.add_argument("--sweeps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the ADI and uneven-batch measurements")
     ap.add_argument("--profile-case", default=None,
                     help="comma list of refine_x,refine_z,fp64_x,fp64_z: two launches each on ~256 MiB fields "
                          "(n = 512 along the solved axis), for ncu captures; prints nothing to time")

@@ -2,15 +2,19 @@
 // factor tables in the padded chunk layout, dispatch to the kernel
 // instances (ntk_refine_m*.cu, kernel in ntk_refine.cuh).
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "ntk_refine.cuh"
 
 namespace ntk {
 
+
 struct RefineState {
   int M = 0;
   int n_pad = 0;
+  int ncls = 32;
+  unsigned char cls[32] = {0};
   float* d_tab = nullptr;
   unsigned* d_status = nullptr;
   bool pow2 = false;
@@ -56,29 +60,62 @@ int Plan::init_refine() {
   st->n_pad = 32 * M;
   // FP32 tables in the padded chunk layout (ChunkTabs); rows >= n are
   // identity rows (l = w = 0, g = 1)
-  const int TS = 32 * (M + 1);
   std::vector<double> L(32 * M, 0.0), G(32 * M, 1.0), Wv(32 * M, 0.0);
   for (int r = 0; r < n; ++r) {
     L[r] = lu_l[r];
     G[r] = 1.0 / lu_u[r];
     Wv[r] = (r < n - 1 ? mat.c(r) : 0.0) / lu_u[r];
   }
-  std::vector<float> tab(6 * (size_t)TS, 0.f);  // gwp[TS] (4 floats each) | l[TS] | psi[TS]
+  // per-lane chunk tables: g, w, phi, l, psi for each of the M rows
+  std::vector<std::vector<float>> lane_tab(32, std::vector<float>(5 * (size_t)M, 0.f));
   for (int j = 0; j < 32; ++j) {
+    std::vector<float>& t = lane_tab[j];
     double phi = 1.0;
     for (int k = 0; k < M; ++k) {
-      const int r = j * M + k, e = j * (M + 1) + k;
+      const int r = j * M + k;
       phi *= -L[r];
-      tab[4 * e + 0] = (float)G[r];
-      tab[4 * e + 1] = (float)Wv[r];
-      tab[4 * e + 2] = (float)phi;
-      tab[4 * TS + e] = (float)L[r];
+      t[5 * k + 0] = (float)G[r];
+      t[5 * k + 1] = (float)Wv[r];
+      t[5 * k + 2] = (float)phi;
+      t[5 * k + 3] = (float)L[r];
     }
     double psi = 1.0;
     for (int k = M - 1; k >= 0; --k) {
-      const int r = j * M + k, e = j * (M + 1) + k;
+      const int r = j * M + k;
       psi *= -Wv[r];
-      tab[5 * TS + e] = (float)psi;
+      t[5 * k + 4] = (float)psi;
+    }
+  }
+  // lanes with bitwise identical tables share one class
+  std::vector<int> rep;
+  for (int j = 0; j < 32; ++j) {
+    int c = -1;
+    for (size_t q = 0; q < rep.size() && c < 0; ++q)
+      if (std::memcmp(lane_tab[rep[q]].data(), lane_tab[j].data(), sizeof(float) * 5 * M) == 0) c = (int)q;
+    if (c < 0) {
+      c = (int)rep.size();
+      rep.push_back(j);
+    }
+    st->cls[j] = (unsigned char)c;
+  }
+  st->ncls = (int)rep.size();
+  const int TC = st->ncls * (M + 1);
+  // lane map (32 ints) | gwp[TC] (4 floats each) | l[TC] | psi[TC]
+  std::vector<float> tab(32 + 6 * (size_t)TC, 0.f);
+  for (int j = 0; j < 32; ++j) {
+    const int c = st->cls[j];
+    std::memcpy(&tab[j], &c, sizeof(int));
+  }
+  float* tf = tab.data() + 32;
+  for (int c = 0; c < st->ncls; ++c) {
+    const std::vector<float>& t = lane_tab[rep[c]];
+    for (int k = 0; k < M; ++k) {
+      const int e = c * (M + 1) + k;
+      tf[4 * e + 0] = t[5 * k + 0];
+      tf[4 * e + 1] = t[5 * k + 1];
+      tf[4 * e + 2] = t[5 * k + 2];
+      tf[4 * TC + e] = t[5 * k + 3];
+      tf[5 * TC + e] = t[5 * k + 4];
     }
   }
   int rc = cuda_status(cudaMalloc(&st->d_tab, tab.size() * sizeof(float)), "cudaMalloc(refine tables)");
@@ -138,6 +175,7 @@ int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsPar
   }
   RefineArgs ra;
   ra.tab = refine->d_tab;
+  ra.ncls = refine->ncls;
   ra.ai = to_dw(mat.ai);
   ra.bi = to_dw(mat.bi);
   ra.ci = to_dw(mat.ci);

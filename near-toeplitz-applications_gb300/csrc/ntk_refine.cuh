@@ -49,7 +49,15 @@ struct DW {
 };
 
 struct RefineArgs {
-  const float* tab = nullptr;  // per padded row: [gwp float4][l][psi] (see ChunkTabs)
+  // FP32 factor tables per lane class: lanes whose chunks see identical
+  // factors share one table (typically three classes: the first chunk, the
+  // interior chunks, the chunk holding row n-1).  Layout: [class of each
+  // lane: 32 ints] [gwp float4 x ncls*(M+1)] [l x ncls*(M+1)] [psi x
+  // ncls*(M+1)]; class c's chunk starts at entry c*(M+1).  (The lane map
+  // lives in device memory: indexing a kernel parameter by lane would force
+  // a local copy of the whole parameter block.)
+  const float* tab = nullptr;
+  int ncls = 32;
   DW ai, bi, ci;               // interior row coefficients
   int nh = 1, nt = 1;          // special rows: head 0..nh-1, tail n-nt..n-1
   DW hd[2][3];                 // head rows (a, b, c), double-word
@@ -195,13 +203,19 @@ struct RefineOcc {
   static constexpr int value = (M <= 16) ? NTK_REFINE_OCC : 1;
 };
 
-// Shared-memory footprint of one CTA: W padded system tiles, the tables
-// (l and psi: 2 floats, gwp: a float4, per padded row) and the double-word
-// boundary right-hand sides (rows 0 and n-1 of each system).
+// Shared-memory footprint of one CTA: two buffers of W padded system tiles,
+// the class tables (l and psi: 2 floats, gwp: a float4, per padded row)
+// and, per buffer, the boundary stencils' inputs (3 doubles) and their
+// double-word results for rows 0 and n-1 of each system.
+#ifndef REFINE_GROUPS_PER_CTA
+#define REFINE_GROUPS_PER_CTA 2
+#endif
+constexpr int kRefineBuffers = REFINE_GROUPS_PER_CTA > 1 ? 2 : 1;
 template <int M>
-__host__ __device__ constexpr size_t refine_smem(int W) {
-  return (size_t)W * sys_pitch<M>() * sizeof(double) + (size_t)32 * (M + 1) * (2 * sizeof(float) + sizeof(float4)) +
-         (size_t)2 * W * sizeof(float2);
+__host__ __device__ constexpr size_t refine_smem(int W, int ncls) {
+  return (((size_t)kRefineBuffers * W * sys_pitch<M>() * sizeof(double) + 15) & ~(size_t)15) +
+         (size_t)ncls * (M + 1) * (2 * sizeof(float) + sizeof(float4)) +
+         (size_t)kRefineBuffers * 2 * W * (sizeof(float2) + 3 * sizeof(double));
 }
 
 // Offset of system s's first unknown: (s / ni) * os + (s % ni) * is, with
@@ -229,301 +243,417 @@ __device__ __forceinline__ double scaled_out(float h, float l, const RefineArgs&
   return dw_to_f64(h, l);
 }
 
+// s * (x + d) for an FP32 solution x and its FP32 correction d, as an FP64
+// value: s_h * x is split exactly (TwoProd) and the small terms s_h * d and
+// s_l * x are added to its error (s_l * d lies below the double-word's
+// precision), then the pair is normalised and assembled.
+__device__ __forceinline__ double corrected_out(float x, float d, const RefineArgs& ra) {
+  float h, e;
+  if (ra.unit_scale) {
+    two_sum(x, d, h, e);
+  } else {
+    const float p = __fmul_rn(ra.s.h, x);
+    float t = __fmaf_rn(ra.s.h, x, -p);
+    t = __fmaf_rn(ra.s.h, d, t);
+    t = __fmaf_rn(ra.s.l, x, t);
+    fast_two_sum(p, t, h, e);
+  }
+  return dw_to_f64(h, e);
+}
+
+// One system, solved by one warp in place in its padded tile trow: RHS
+// (bndw: the double-word right-hand sides of rows 0 and n-1), FP32 solve,
+// refinement sweeps; the FP64 result is left in the tile slots.
 template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY>
-__global__ void __launch_bounds__(256, RefineOcc<M>::value)
-    refine_kernel(const double* in, double* out, int n, Batch b, RefineArgs ra) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int P = sys_pitch<M>();
-  constexpr int TS = 32 * (M + 1);        // table entries
-  constexpr int QSTEP = (32 / M) * (M + 1);  // tile_off(r + 32) - tile_off(r)
-  const int W = blockDim.x >> 5;
-  double* tile = reinterpret_cast<double*>(smem_raw);
-  float4* tgwp = reinterpret_cast<float4*>(tile + (size_t)W * P);  // 16-byte aligned: W*P*8 = W*(32(M+1)+1)*8
-  float* tl_all = reinterpret_cast<float*>(tgwp + TS);
-  float* tpsi_all = tl_all + TS;
-  float2* bnd = reinterpret_cast<float2*>(tpsi_all + TS);  // [2 * W]: rows 0 and n-1
-  const int tid = threadIdx.x;
-  const int warp = tid >> 5;
-  const unsigned lane = tid & 31;
-  const long long s0 = (long long)blockIdx.x * W;
-  const int wcount = (int)((b.nsys - s0) < W ? (b.nsys - s0) : W);
-  unsigned range = 0;
+__device__ __forceinline__ void refine_system(double* trow, const float2* bndw, const ChunkTabs& tabs, int n,
+                                              const RefineArgs& ra, unsigned lane, unsigned& range) {
+  const int j = lane;
+  const int r0 = j * M;
+  const int cb = j * (M + 1);  // this lane's chunk in the tile
+  float2* drow = reinterpret_cast<float2*>(trow);
+  const int n1 = n - 1;
+  const bool tail_here = (r0 <= n1) && (n1 < r0 + M);  // owns row n-1
+  float x[M];
 
-  // tables: ra.tab holds [gwp (4 floats) | l | psi] per padded row
-  {
-    const float4* g4 = reinterpret_cast<const float4*>(ra.tab);
-    for (int i = tid; i < TS; i += blockDim.x) tgwp[i] = g4[i];
-    const float* lp = ra.tab + 4 * TS;
-    for (int i = tid; i < 2 * TS; i += blockDim.x) tl_all[i] = lp[i];
-  }
-
-  // ---- stage the W systems: coalesced cp.async, all copies in flight at once ----
-  // Every thread copies M rows; the row of its q-th copy is rb + 32q, with
-  // rb = lane (x: one system per warp) or tid / W (strided: blockDim / W ==
-  // 32), so its tile slot is tile_off(rb) + q * QSTEP.  The same thread
-  // stores the same rows at the end.
-  const int sw = (b.es == 1) ? warp : tid % W;  // system (within the CTA) this thread copies
-  const int rb = (b.es == 1) ? (int)lane : tid / W;
-  if (sw < wcount) {
-    const double* gsrc = in + sys_offset(s0 + sw, b) + (long long)rb * b.es;
-    double* tslot = tile + (size_t)sw * P + tile_off<M>(rb);
-    const long long gstep = 32LL * b.es;
+  // ---- RHS in double-word, written back into the tile slots ----
+  if (RHS == RHS_COMPACT) {
+    // D_r = f_{r+1} - f_{r-1} is formed in FP64 (one DADD, as in the FP64
+    // path) and then split: a double-word split of f itself keeps only
+    // ~2^-47 |f|, too coarse when f_{r+1} and f_{r-1} nearly cancel.  Rows 0
+    // and n-1 take the boundary stencils staged in bnd.
+    const double fleft = (j > 0) ? trow[tile_off<M>(r0 - 1)] : 0.0;
+    const double fright = (j < 31) ? trow[tile_off<M>(r0 + M)] : 0.0;
+    __syncwarp();  // the neighbours' halo reads happen before any slot is rewritten
+    double fprev = fleft, fcur = trow[cb];
 #pragma unroll
-    for (int q = 0; q < M; ++q) {
-      const bool ok = !PAD || rb + 32 * q < n;
-      cp_async8(tslot + q * QSTEP, ok ? gsrc + q * gstep : in, ok ? 8u : 0u);
-    }
-  }
-  // The compact scheme's one-sided boundary stencils (compact/rhs.py:21-31)
-  // in FP64, for all W systems at once by the first warp (lane 2w: row 0 of
-  // system w, lane 2w+1: row n-1), read straight from global memory while the
-  // copies are in flight: one set of FP64 instructions per CTA instead of
-  // one per system.
-  if (RHS == RHS_COMPACT && warp == 0) {
-    const int w = (int)(lane >> 1);
-    if (w < wcount) {
-      const bool tl = lane & 1;
-      const double* f = in + sys_offset(s0 + w, b);
-      const long long e = b.es;
-      const long long q0 = tl ? (long long)(n - 1) * e : 0, q1 = tl ? (long long)(n - 2) * e : e,
-                      q2 = tl ? (long long)(n - 3) * e : 2 * e;
-      const double v = (tl ? ra.sigmaN : ra.sigma0) * ((-5.0 * __ldg(f + q0) + 4.0 * __ldg(f + q1)) + __ldg(f + q2));
+    for (int k = 0; k < M; ++k) {
+      const double fnext = (k < M - 1) ? trow[cb + k + 1] : fright;
       float h, l;
-      split_f64(v, h, l, range);
+      split_f64(fnext - fprev, h, l, range);
       fast_two_sum(h, l, h, l);
-      bnd[lane] = make_float2(h, l);
+      x[k] = h;
+      drow[cb + k] = make_float2(h, l);
+      fprev = fcur;
+      fcur = fnext;
+    }
+    if (j == 0) {
+      const float2 d0 = bndw[0];
+      x[0] = d0.x;
+      drow[cb + 0] = d0;
+    }
+    if (tail_here) {
+      const float2 d1 = bndw[1];
+      const float h = d1.x;
+      if (!PAD) {
+        x[M - 1] = h;
+      } else {
+#pragma unroll
+        for (int k = 0; k < M; ++k)
+          if (r0 + k == n1) x[k] = h;
+      }
+      drow[tile_off<M>(n1)] = d1;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      float h, l;
+      split_f64(trow[cb + k], h, l, range);
+      fast_two_sum(h, l, h, l);  // h = d rounded to FP32
+      x[k] = h;
+      drow[cb + k] = make_float2(h, l);
     }
   }
-  cp_async_wait_all();
-  __syncthreads();
 
-  if (warp < wcount) {
-    double* trow = tile + (size_t)warp * P;
-    const int j = lane;
-    const int r0 = j * M;
-    const int cb = j * (M + 1);  // this lane's chunk in the tile
-    float2* drow = reinterpret_cast<float2*>(trow);
-    ChunkTabs tabs;
-    tabs.l = tl_all + cb;
-    tabs.gwp = tgwp + cb;
-    tabs.psi = tpsi_all + cb;
-    const int n1 = n - 1;
-    const bool tail_here = (r0 <= n1) && (n1 < r0 + M);  // owns row n-1
-    float x[M];
+  // ---- FP32 solve ----
+  chunk_solve<M, DECAY>(x, tabs, lane);
 
-    // ---- RHS in double-word, written back into the tile slots ----
-    if (RHS == RHS_COMPACT) {
-      // D_r = f_{r+1} - f_{r-1} is formed in FP64 (one DADD, as in the FP64
-      // path) and then split: a double-word split of f itself keeps only
-      // ~2^-47 |f|, too coarse when f_{r+1} and f_{r-1} nearly cancel.  Rows 0
-      // and n-1 take the boundary stencils staged in bnd.
-      const double fleft = (j > 0) ? trow[tile_off<M>(r0 - 1)] : 0.0;
-      const double fright = (j < 31) ? trow[tile_off<M>(r0 + M)] : 0.0;
-      __syncwarp();  // the neighbours' halo reads happen before any slot is rewritten
-      double fprev = fleft, fcur = trow[cb];
+  // ---- refinement sweeps; the last one writes the FP64 result ----
+  float xl[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) xl[k] = 0.f;
+  if (SWEEPS == 0) {
+#pragma unroll
+    for (int k = 0; k < M; ++k) trow[cb + k] = scaled_out(x[k], 0.f, ra);
+  }
+#pragma unroll
+  for (int sweep = 0; sweep < SWEEPS; ++sweep) {
+    // every lane executes every shuffle (full mask); edges are zeroed after
+    float xleft = __shfl_up_sync(FULL, x[M - 1], 1);
+    float xright = __shfl_down_sync(FULL, x[0], 1);
+    if (j == 0) xleft = 0.f;
+    if (j == 31) xright = 0.f;
+    float lleft = 0.f, lright = 0.f;
+    if (sweep > 0) {  // sweep is warp-uniform
+      lleft = __shfl_up_sync(FULL, xl[M - 1], 1);
+      lright = __shfl_down_sync(FULL, xl[0], 1);
+      if (j == 0) lleft = 0.f;
+      if (j == 31) lright = 0.f;
+    }
+    float r[M];
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      const float2 d = drow[cb + k];
+      const float xm = (k == 0) ? xleft : x[k - (k > 0)];
+      const float xp = (k == M - 1) ? xright : x[k + (k < M - 1)];
+      if (sweep == 0) {
+        r[k] = residual_row<POW2, false>(d.x, d.y, xm, x[k], xp, 0.f, 0.f, 0.f, ra.ai, ra.bi, ra.ci);
+      } else {
+        const float lm = (k == 0) ? lleft : xl[k - (k > 0)];
+        const float lp = (k == M - 1) ? lright : xl[k + (k < M - 1)];
+        r[k] = residual_row<POW2, true>(d.x, d.y, xm, x[k], xp, lm, xl[k], lp, ra.ai, ra.bi, ra.ci);
+      }
+    }
+    // rows with their own coefficients, in double-word FP32 like the
+    // interior: head rows sit in lane 0 at compile-time positions
+    if (j == 0) {
+#pragma unroll
+      for (int k = 0; k < 2 && k < M; ++k) {
+        if (k < ra.nh) {
+          const float2 d = drow[cb + k];
+          const float xm = (k == 0) ? 0.f : x[k - (k > 0)];
+          const float lm = (k == 0) ? 0.f : xl[k - (k > 0)];
+          const float xp = (k == M - 1) ? xright : x[k + (k < M - 1)];
+          const float lp = (k == M - 1) ? lright : xl[k + (k < M - 1)];
+          r[k] = residual_row<false, true>(d.x, d.y, xm, x[k], xp, lm, xl[k], lp, ra.hd[k][0], ra.hd[k][1],
+                                           ra.hd[k][2]);
+        }
+      }
+    }
+    // tail rows
+    if (r0 + M > n - ra.nt && r0 < n) {
+      if (!PAD) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int k = M - 1 - q;  // row n-1-q
+          if (q < ra.nt && k >= 0) {
+            const int ti = ra.nt - 1 - q;
+            const float2 d = drow[cb + k];
+            const float xm = (k == 0) ? xleft : x[k - (k > 0)];
+            const float lm = (k == 0) ? lleft : xl[k - (k > 0)];
+            const float xp = (q == 0) ? 0.f : x[k + (k < M - 1)];
+            const float lp = (q == 0) ? 0.f : xl[k + (k < M - 1)];
+            r[k] = residual_row<false, true>(d.x, d.y, xm, x[k], xp, lm, xl[k], lp, ra.td[ti][0], ra.td[ti][1],
+                                             ra.td[ti][2]);
+          }
+        }
+      } else {
+        // runtime position: gather the needed values with selects
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int row = n1 - q;
+          if (q < ra.nt && row >= r0 && row < r0 + M) {
+            const int kk = row - r0;
+            float xh0 = 0.f, xl0 = 0.f, xhm = 0.f, xlm = 0.f, xhp = 0.f, xlp = 0.f;
+#pragma unroll
+            for (int k = 0; k < M; ++k) {
+              if (k == kk) {
+                xh0 = x[k];
+                xl0 = xl[k];
+              }
+              if (k == kk - 1) {
+                xhm = x[k];
+                xlm = xl[k];
+              }
+              if (k == kk + 1) {
+                xhp = x[k];
+                xlp = xl[k];
+              }
+            }
+            if (kk == 0) {
+              xhm = xleft;
+              xlm = lleft;
+            }
+            if (kk == M - 1) {
+              xhp = xright;
+              xlp = lright;
+            }
+            if (q == 0) {
+              xhp = 0.f;
+              xlp = 0.f;
+            }
+            const int ti = ra.nt - 1 - q;
+            const float2 d = drow[tile_off<M>(row)];
+            const float rr = residual_row<false, true>(d.x, d.y, xhm, xh0, xhp, xlm, xl0, xlp, ra.td[ti][0],
+                                                       ra.td[ti][1], ra.td[ti][2]);
+#pragma unroll
+            for (int k = 0; k < M; ++k)
+              if (k == kk) r[k] = rr;
+          }
+        }
+      }
+    }
+    chunk_solve<M, DECAY>(r, tabs, lane);
+    if (sweep + 1 < SWEEPS) {
+      // x + delta as a normalised double-word for the next sweep
 #pragma unroll
       for (int k = 0; k < M; ++k) {
-        const double fnext = (k < M - 1) ? trow[cb + k + 1] : fright;
-        float h, l;
-        split_f64(fnext - fprev, h, l, range);
-        fast_two_sum(h, l, h, l);
-        x[k] = h;
-        drow[cb + k] = make_float2(h, l);
-        fprev = fcur;
-        fcur = fnext;
-      }
-      if (j == 0) {
-        const float2 d0 = bnd[2 * warp];
-        x[0] = d0.x;
-        drow[cb + 0] = d0;
-      }
-      if (tail_here) {
-        const float2 d1 = bnd[2 * warp + 1];
-        const float h = d1.x;
-        if (!PAD) {
-          x[M - 1] = h;
-        } else {
-#pragma unroll
-          for (int k = 0; k < M; ++k)
-            if (r0 + k == n1) x[k] = h;
-        }
-        drow[tile_off<M>(n1)] = d1;
+        float h, e;
+        two_sum(x[k], r[k], h, e);
+        e += xl[k];
+        fast_two_sum(h, e, x[k], xl[k]);
       }
     } else {
+      // last sweep: s * (x + delta) straight to the FP64 output slot
 #pragma unroll
       for (int k = 0; k < M; ++k) {
-        float h, l;
-        split_f64(trow[cb + k], h, l, range);
-        fast_two_sum(h, l, h, l);  // h = d rounded to FP32
-        x[k] = h;
-        drow[cb + k] = make_float2(h, l);
-      }
-    }
-
-    // ---- FP32 solve ----
-    chunk_solve<M, DECAY>(x, tabs, lane);
-
-    // ---- refinement sweeps; the last one writes the FP64 result ----
-    float xl[M];
-#pragma unroll
-    for (int k = 0; k < M; ++k) xl[k] = 0.f;
-    if (SWEEPS == 0) {
-#pragma unroll
-      for (int k = 0; k < M; ++k) trow[cb + k] = scaled_out(x[k], 0.f, ra);
-    }
-#pragma unroll
-    for (int sweep = 0; sweep < SWEEPS; ++sweep) {
-      // every lane executes every shuffle (full mask); edges are zeroed after
-      float xleft = __shfl_up_sync(FULL, x[M - 1], 1);
-      float xright = __shfl_down_sync(FULL, x[0], 1);
-      if (j == 0) xleft = 0.f;
-      if (j == 31) xright = 0.f;
-      float lleft = 0.f, lright = 0.f;
-      if (sweep > 0) {  // sweep is warp-uniform
-        lleft = __shfl_up_sync(FULL, xl[M - 1], 1);
-        lright = __shfl_down_sync(FULL, xl[0], 1);
-        if (j == 0) lleft = 0.f;
-        if (j == 31) lright = 0.f;
-      }
-      float r[M];
-#pragma unroll
-      for (int k = 0; k < M; ++k) {
-        const float2 d = drow[cb + k];
-        const float xm = (k == 0) ? xleft : x[k - (k > 0)];
-        const float xp = (k == M - 1) ? xright : x[k + (k < M - 1)];
         if (sweep == 0) {
-          r[k] = residual_row<POW2, false>(d.x, d.y, xm, x[k], xp, 0.f, 0.f, 0.f, ra.ai, ra.bi, ra.ci);
+          trow[cb + k] = corrected_out(x[k], r[k], ra);
         } else {
-          const float lm = (k == 0) ? lleft : xl[k - (k > 0)];
-          const float lp = (k == M - 1) ? lright : xl[k + (k < M - 1)];
-          r[k] = residual_row<POW2, true>(d.x, d.y, xm, x[k], xp, lm, xl[k], lp, ra.ai, ra.bi, ra.ci);
-        }
-      }
-      // rows with their own coefficients, in double-word FP32 like the
-      // interior: head rows sit in lane 0 at compile-time positions
-      if (j == 0) {
-#pragma unroll
-        for (int k = 0; k < 2 && k < M; ++k) {
-          if (k < ra.nh) {
-            const float2 d = drow[cb + k];
-            const float xm = (k == 0) ? 0.f : x[k - (k > 0)];
-            const float lm = (k == 0) ? 0.f : xl[k - (k > 0)];
-            const float xp = (k == M - 1) ? xright : x[k + (k < M - 1)];
-            const float lp = (k == M - 1) ? lright : xl[k + (k < M - 1)];
-            r[k] = residual_row<false, true>(d.x, d.y, xm, x[k], xp, lm, xl[k], lp, ra.hd[k][0], ra.hd[k][1],
-                                             ra.hd[k][2]);
-          }
-        }
-      }
-      // tail rows
-      if (r0 + M > n - ra.nt && r0 < n) {
-        if (!PAD) {
-#pragma unroll
-          for (int q = 0; q < 2; ++q) {
-            const int k = M - 1 - q;  // row n-1-q
-            if (q < ra.nt && k >= 0) {
-              const int ti = ra.nt - 1 - q;
-              const float2 d = drow[cb + k];
-              const float xm = (k == 0) ? xleft : x[k - (k > 0)];
-              const float lm = (k == 0) ? lleft : xl[k - (k > 0)];
-              const float xp = (q == 0) ? 0.f : x[k + (k < M - 1)];
-              const float lp = (q == 0) ? 0.f : xl[k + (k < M - 1)];
-              r[k] = residual_row<false, true>(d.x, d.y, xm, x[k], xp, lm, xl[k], lp, ra.td[ti][0], ra.td[ti][1],
-                                               ra.td[ti][2]);
-            }
-          }
-        } else {
-          // runtime position: gather the needed values with selects
-#pragma unroll
-          for (int q = 0; q < 2; ++q) {
-            const int row = n1 - q;
-            if (q < ra.nt && row >= r0 && row < r0 + M) {
-              const int kk = row - r0;
-              float xh0 = 0.f, xl0 = 0.f, xhm = 0.f, xlm = 0.f, xhp = 0.f, xlp = 0.f;
-#pragma unroll
-              for (int k = 0; k < M; ++k) {
-                if (k == kk) {
-                  xh0 = x[k];
-                  xl0 = xl[k];
-                }
-                if (k == kk - 1) {
-                  xhm = x[k];
-                  xlm = xl[k];
-                }
-                if (k == kk + 1) {
-                  xhp = x[k];
-                  xlp = xl[k];
-                }
-              }
-              if (kk == 0) {
-                xhm = xleft;
-                xlm = lleft;
-              }
-              if (kk == M - 1) {
-                xhp = xright;
-                xlp = lright;
-              }
-              if (q == 0) {
-                xhp = 0.f;
-                xlp = 0.f;
-              }
-              const int ti = ra.nt - 1 - q;
-              const float2 d = drow[tile_off<M>(row)];
-              const float rr = residual_row<false, true>(d.x, d.y, xhm, xh0, xhp, xlm, xl0, xlp, ra.td[ti][0],
-                                                         ra.td[ti][1], ra.td[ti][2]);
-#pragma unroll
-              for (int k = 0; k < M; ++k)
-                if (k == kk) r[k] = rr;
-            }
-          }
-        }
-      }
-      chunk_solve<M, DECAY>(r, tabs, lane);
-      if (sweep + 1 < SWEEPS) {
-        // x + delta as a normalised double-word for the next sweep
-#pragma unroll
-        for (int k = 0; k < M; ++k) {
           float h, e;
           two_sum(x[k], r[k], h, e);
           e += xl[k];
-          fast_two_sum(h, e, x[k], xl[k]);
-        }
-      } else {
-        // last sweep: x + delta straight to the FP64 output slot
-#pragma unroll
-        for (int k = 0; k < M; ++k) {
-          float h, e;
-          two_sum(x[k], r[k], h, e);
-          if (sweep > 0) {
-            e += xl[k];
-            fast_two_sum(h, e, h, e);
-          }
+          fast_two_sum(h, e, h, e);
           trow[cb + k] = scaled_out(h, e, ra);
         }
       }
     }
   }
-  if (range && ra.status) atomicOr(ra.status, 1u);
-  __syncthreads();
+}
 
-  // ---- store: each thread writes back the rows it staged ----
-  if (sw < wcount) {
-    double* gdst = out + sys_offset(s0 + sw, b) + (long long)rb * b.es;
-    const double* tslot = tile + (size_t)sw * P + tile_off<M>(rb);
+// ---- staging map of the persistent kernel ----
+// Every thread copies M rows of one system, rows rb + 32q, with rb = lane
+// (contiguous systems: one system per warp, 256-byte rows of copies) or
+// tid / W (strided systems: lanes walk W adjacent systems, blockDim / W ==
+// 32); slot tile_off(rb) + q * QSTEP.  The same thread stores the same rows
+// at the end, so a buffer is reused without a barrier between the stores of
+// one group and the copies of the group after next.
+__device__ __forceinline__ int group_count(const Batch& b, int grp, int W) {
+  const long long left = b.nsys - (long long)grp * W;
+  return (int)(left < W ? left : W);
+}
+__device__ __forceinline__ int map_sw(const Batch& b, int W) {
+  return (b.es == 1) ? (int)(threadIdx.x >> 5) : (int)threadIdx.x % W;
+}
+__device__ __forceinline__ int map_rb(const Batch& b, int W) {
+  return (b.es == 1) ? (int)(threadIdx.x & 31) : (int)threadIdx.x / W;
+}
+
+// issue the copies of group grp into buffer buf (one cp.async group)
+template <int M, int RHS, bool PAD>
+__device__ __forceinline__ void refine_stage(const double* in, double* tiles, double* braw, int n, const Batch& b,
+                                             int grp, int buf, int W) {
+  constexpr int P = sys_pitch<M>();
+  constexpr int QSTEP = (32 / M) * (M + 1);
+  const int wc = group_count(b, grp, W);
+  const int sw = map_sw(b, W), rb = map_rb(b, W);
+  if (sw < wc) {
+    const double* gsrc = in + sys_offset((long long)grp * W + sw, b) + (long long)rb * b.es;
+    double* tslot = tiles + (size_t)buf * W * P + sw * P + tile_off<M>(rb);
+    const long long gstep = 32LL * b.es;
+    // the source address is advanced step by step (offsets q * gstep would be
+    // hoisted out of the group loop and held in registers)
+#pragma unroll
+    for (int q = 0; q < M; ++q) {
+      const bool ok = !PAD || rb + 32 * q < n;
+      cp_async8(tslot + q * QSTEP, ok ? gsrc : in, ok ? 8u : 0u);
+      gsrc += gstep;
+    }
+  }
+  // inputs of the one-sided boundary stencils (compact/rhs.py:21-31): first
+  // warp, lane 2w: rows 0..2 of system w, lane 2w+1: rows n-1..n-3
+  const unsigned lane = threadIdx.x & 31;
+  if (RHS == RHS_COMPACT && threadIdx.x < 32 && (int)(lane >> 1) < wc) {
+    const bool tl = lane & 1;
+    const double* f = in + sys_offset((long long)grp * W + (lane >> 1), b);
+    const long long e = b.es;
+    double* dst = braw + ((size_t)buf * 2 * W + lane) * 3;
+    cp_async8(dst + 0, f + (tl ? (long long)(n - 1) * e : 0), 8u);
+    cp_async8(dst + 1, f + (tl ? (long long)(n - 2) * e : e), 8u);
+    cp_async8(dst + 2, f + (tl ? (long long)(n - 3) * e : 2 * e), 8u);
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// first warp, once its copies of group grp have landed: the boundary
+// stencils in FP64, one set of FP64 instructions for all W systems
+template <int RHS>
+__device__ __forceinline__ void refine_boundary(const double* braw, float2* bnd, const Batch& b, const RefineArgs& ra,
+                                                int grp, int buf, int W, unsigned& range) {
+  const unsigned lane = threadIdx.x & 31;
+  if (RHS == RHS_COMPACT && (int)(lane >> 1) < group_count(b, grp, W)) {
+    const double* r = braw + ((size_t)buf * 2 * W + lane) * 3;
+    const double v = ((lane & 1) ? ra.sigmaN : ra.sigma0) * ((-5.0 * r[0] + 4.0 * r[1]) + r[2]);
+    float h, l;
+    split_f64(v, h, l, range);
+    fast_two_sum(h, l, h, l);
+    bnd[(size_t)buf * 2 * W + lane] = make_float2(h, l);
+  }
+}
+
+template <int M, bool PAD>
+__device__ __forceinline__ void refine_store(double* out, const double* tiles, int n, const Batch& b, int grp, int buf,
+                                             int W) {
+  constexpr int P = sys_pitch<M>();
+  constexpr int QSTEP = (32 / M) * (M + 1);
+  const int wc = group_count(b, grp, W);
+  const int sw = map_sw(b, W), rb = map_rb(b, W);
+  if (sw < wc) {
+    double* gdst = out + sys_offset((long long)grp * W + sw, b) + (long long)rb * b.es;
+    const double* tslot = tiles + (size_t)buf * W * P + sw * P + tile_off<M>(rb);
     const long long gstep = 32LL * b.es;
 #pragma unroll
-    for (int q = 0; q < M; ++q)
-      if (!PAD || rb + 32 * q < n) gdst[q * gstep] = tslot[q * QSTEP];
+    for (int q = 0; q < M; ++q) {
+      if (!PAD || rb + 32 * q < n) *gdst = tslot[q * QSTEP];
+      gdst += gstep;
+    }
   }
+}
+
+// Each CTA solves REFINE_GROUPS_PER_CTA consecutive groups of W systems,
+// double-buffered: while the warps solve one group from one tile buffer,
+// the copies of the next group land in the other, so only the first
+// group's load latency is exposed.  Each thread stages and stores the same
+// slots of its buffer, so the only CTA barriers are "group staged" and
+// "group solved".
+template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY>
+__global__ void __launch_bounds__(256, RefineOcc<M>::value)
+    refine_kernel(const double* in, double* out, int n, Batch b, RefineArgs ra) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int P = sys_pitch<M>();
+  constexpr int QSTEP = (32 / M) * (M + 1);  // tile_off(r + 32) - tile_off(r)
+  const int W = blockDim.x >> 5;
+  const int TC = ra.ncls * (M + 1);  // table entries
+  double* tiles = reinterpret_cast<double*>(smem_raw);  // [buffers][W][P]
+  float4* tgwp = reinterpret_cast<float4*>(smem_raw + (((size_t)kRefineBuffers * W * P * sizeof(double) + 15) &
+                                                       ~(size_t)15));
+  float* tl_all = reinterpret_cast<float*>(tgwp + TC);
+  float* tpsi_all = tl_all + TC;
+  float2* bnd = reinterpret_cast<float2*>(tpsi_all + TC);              // [buffers][2W]: rows 0, n-1
+  double* braw = reinterpret_cast<double*>(bnd + kRefineBuffers * 2 * W);  // [buffers][2W][3]: stencil inputs
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const unsigned lane = tid & 31;
+  // group indices fit in 32 bits (the launcher checks nsys / W < 2^31)
+  const int ngroups = (int)((b.nsys + W - 1) / W);
+  const int g = blockIdx.x * REFINE_GROUPS_PER_CTA;
+  if (g >= ngroups) return;  // whole CTA
+  unsigned range = 0;
+
+  const int cbase = __ldg(reinterpret_cast<const int*>(ra.tab) + lane) * (M + 1);
+  {
+    const float4* g4 = reinterpret_cast<const float4*>(ra.tab + 32);
+    for (int i = tid; i < TC; i += blockDim.x) tgwp[i] = g4[i];
+    const float* lp = ra.tab + 32 + 4 * TC;
+    for (int i = tid; i < 2 * TC; i += blockDim.x) tl_all[i] = lp[i];
+  }
+
+  // The group sequence is unrolled at compile time: a run-time group loop
+  // makes the compiler keep far more values live across its back edge than
+  // the 80 registers of 3 CTAs per SM allow.
+  const int g0 = g;
+#pragma unroll
+  for (int it = 0; it < REFINE_GROUPS_PER_CTA; ++it) {
+    const int buf = it & 1;
+    const int gc = g0 + it;
+    if (it == 0) {
+      refine_stage<M, RHS, PAD>(in, tiles, braw, n, b, gc, 0, W);
+      if (warp == 0) {
+        cp_async_wait_all();
+        __syncwarp();
+        refine_boundary<RHS>(braw, bnd, b, ra, gc, 0, W, range);
+      }
+    }
+    if (gc >= ngroups) break;  // CTA-uniform
+    const int gn = gc + 1;
+    const bool has_next = (it + 1 < REFINE_GROUPS_PER_CTA) && gn < ngroups;  // CTA-uniform
+    if (has_next) {
+      refine_stage<M, RHS, PAD>(in, tiles, braw, n, b, gn, buf ^ 1, W);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      cp_async_wait_all();
+    }
+    __syncthreads();  // group gc staged (all threads' copies), its bnd written
+    if (warp < group_count(b, gc, W)) {
+      ChunkTabs tabs;
+      tabs.l = tl_all + cbase;
+      tabs.gwp = tgwp + cbase;
+      tabs.psi = tpsi_all + cbase;
+      refine_system<M, RHS, SWEEPS, POW2, PAD, DECAY>(tiles + ((size_t)buf * W + warp) * P,
+                                                      bnd + (size_t)buf * 2 * W + 2 * warp, tabs, n, ra, lane, range);
+    }
+    if (warp == 0 && has_next) {
+      cp_async_wait_all();
+      __syncwarp();
+      refine_boundary<RHS>(braw, bnd, b, ra, gn, buf ^ 1, W, range);
+    }
+    __syncthreads();  // group gc solved: results in the tile slots
+    refine_store<M, PAD>(out, tiles, n, b, gc, buf, W);
+  }
+  if (range && ra.status) atomicOr(ra.status, 1u);
 }
 
 template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY>
 int launch_one(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, int W, cudaStream_t st) {
-  const size_t smem = refine_smem<M>(W);
+  const size_t smem = refine_smem<M>(W, ra.ncls);
   auto kern = refine_kernel<M, RHS, SWEEPS, POW2, PAD, DECAY>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(refine_kernel)");
-  const long long blocks = (b.nsys + W - 1) / W;
+  const long long groups = (b.nsys + W - 1) / W;
+  if (groups > 0x7fffffffLL) {
+    set_error("too many systems for one launch");
+    return NTK_ERR_INVALID;
+  }
+  const long long blocks = (groups + REFINE_GROUPS_PER_CTA - 1) / REFINE_GROUPS_PER_CTA;
   kern<<<(unsigned)blocks, W * 32, smem, st>>>(in, out, n, b, ra);
   return cuda_status(cudaGetLastError(), "refine_kernel");
 }

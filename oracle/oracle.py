@@ -246,6 +246,24 @@ def near_toeplitz_bands(n, coeffs):
     return a, b, c
 
 
+def near_toeplitz_bands_general(n, interior, head, tail):
+    """Diagonals of one system of an uneven batch (ntk_batch_create's model,
+    which generalises neato.py:136-138 to two special rows per end): rows 0
+    and 1 from head, rows n-2 and n-1 from tail, interior (a, b, c) between;
+    for n = 3 the shared middle row is head's second row."""
+    a = np.full(n, float(interior[0]))
+    b = np.full(n, float(interior[1]))
+    c = np.full(n, float(interior[2]))
+    for r in range(2):
+        if n - 2 + r >= 2:
+            a[n - 2 + r], b[n - 2 + r], c[n - 2 + r] = tail[r]
+    for r in range(2):
+        a[r], b[r], c[r] = head[r]
+    a[0] = 0.0
+    c[-1] = 0.0
+    return a, b, c
+
+
 def compact_rhs_numpy(f, h, axis):
     """compact/rhs.py:21-36 along `axis`, vectorised NumPy."""
     f = np.moveaxis(np.asarray(f, dtype=np.float64), axis, -1)
