@@ -76,7 +76,7 @@ __device__ __forceinline__ double dw_to_f64(float hi, float lo) {
   const unsigned eh = bh & 0x7f800000u;
   // 2^(46 - e_hi) carrying hi's sign: k > 0 moves away from zero
   const float sc = __uint_as_float(((300u << 23) - eh) | (bh & 0x80000000u));
-  const float t = __fadd_rn(__fmul_rn(lo, sc), 12582912.0f);
+  const float t = __fmaf_rn(lo, sc, 12582912.0f);  // one rounding: k = round(lo * sc)
   int k = (int)(__float_as_uint(t) - 0x4b400000u);
   if ((bh & 0x007fffffu) == 0u && k < 0) k *= 2;
   const unsigned dhi = ((bh & 0x7fffffffu) >> 3) + (896u << 20);

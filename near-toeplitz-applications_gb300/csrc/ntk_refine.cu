@@ -99,9 +99,10 @@ int Plan::init_refine() {
     st->cls[j] = (unsigned char)c;
   }
   st->ncls = (int)rep.size();
-  const int TC = st->ncls * (M + 1);
-  // lane map (32 ints) | gwp[TC] (4 floats each) | l[TC] | psi[TC]
-  std::vector<float> tab(32 + 6 * (size_t)TC, 0.f);
+  // lane map (32 ints) | per class: groups of four rows as float4s L, G, W,
+  // PHI, PSI (refine_detail::ChunkTabs), pitch class_pitch4
+  const int CP = 5 * (M / 4) + 1;  // refine_detail::class_pitch4<M>()
+  std::vector<float> tab(32 + 4 * (size_t)st->ncls * CP, 0.f);
   for (int j = 0; j < 32; ++j) {
     const int c = st->cls[j];
     std::memcpy(&tab[j], &c, sizeof(int));
@@ -110,12 +111,13 @@ int Plan::init_refine() {
   for (int c = 0; c < st->ncls; ++c) {
     const std::vector<float>& t = lane_tab[rep[c]];
     for (int k = 0; k < M; ++k) {
-      const int e = c * (M + 1) + k;
-      tf[4 * e + 0] = t[5 * k + 0];
-      tf[4 * e + 1] = t[5 * k + 1];
-      tf[4 * e + 2] = t[5 * k + 2];
-      tf[4 * TC + e] = t[5 * k + 3];
-      tf[5 * TC + e] = t[5 * k + 4];
+      float* grp = tf + 4 * ((size_t)c * CP + 5 * (k / 4));
+      const int e = k % 4;
+      grp[0 * 4 + e] = t[5 * k + 3];  // l
+      grp[1 * 4 + e] = t[5 * k + 0];  // g
+      grp[2 * 4 + e] = t[5 * k + 1];  // w
+      grp[3 * 4 + e] = t[5 * k + 2];  // phi
+      grp[4 * 4 + e] = t[5 * k + 4];  // psi
     }
   }
   int rc = cuda_status(cudaMalloc(&st->d_tab, tab.size() * sizeof(float)), "cudaMalloc(refine tables)");

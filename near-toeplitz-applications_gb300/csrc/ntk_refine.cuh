@@ -52,10 +52,10 @@ struct RefineArgs {
   // FP32 factor tables per lane class: lanes whose chunks see identical
   // factors share one table (typically three classes: the first chunk, the
   // interior chunks, the chunk holding row n-1).  Layout: [class of each
-  // lane: 32 ints] [gwp float4 x ncls*(M+1)] [l x ncls*(M+1)] [psi x
-  // ncls*(M+1)]; class c's chunk starts at entry c*(M+1).  (The lane map
-  // lives in device memory: indexing a kernel parameter by lane would force
-  // a local copy of the whole parameter block.)
+  // lane: 32 ints] [class tables: ncls x class_pitch4 float4s, see
+  // ChunkTabs].  (The lane map lives in device memory: indexing a kernel
+  // parameter by lane would force a local copy of the whole parameter
+  // block.)
   const float* tab = nullptr;
   int ncls = 32;
   DW ai, bi, ci;               // interior row coefficients
@@ -85,22 +85,31 @@ __device__ __forceinline__ int tile_off(int r) {
   return (r / M) * (M + 1) + (r % M);
 }
 
-// Per-row FP32 tables of one lane's chunk (padded chunk layout, see tile_off):
-//   l            forward multiplier l_i
-//   gwp = (g, w, phi, 0)  g_i = 1/u_i, w_i = c_i/u_i, phi_i = prod_{chunk start..i} (-l)
-//   psi          prod_{i..chunk end} (-w)
+// Per-row FP32 tables of one lane's chunk, in groups of four rows so one
+// 16-byte shared-memory load serves four rows: group j (rows 4j..4j+3) is
+// five float4s
+//   L[j]    forward multipliers l_i
+//   G[j]    g_i = 1/u_i
+//   Wv[j]   w_i = c_i/u_i
+//   PHI[j]  phi_i = prod_{chunk start..i} (-l)
+//   PSI[j]  psi_i = prod_{i..chunk end} (-w)
 // phi and psi are the responses of a chunk's local sweeps to the carry that
 // enters it; they depend only on the row position, so they are tabulated
 // once per plan instead of being recomputed (and held in registers) per row.
+template <int M>
+__host__ __device__ constexpr int class_pitch4() {
+  return 5 * (M / 4) + 1;  // float4s per lane class (+1: classes start on different banks)
+}
 struct ChunkTabs {
-  const float* l;
-  const float4* gwp;
-  const float* psi;
+  const float4* q;  // this lane's class: 5 float4s per group of four rows
 };
+__device__ __forceinline__ float comp4(const float4& v, int c) {
+  return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
+}
 
 // The table loads of a fully unrolled sweep would otherwise all be hoisted
-// to its start (16 rows x up to 4 floats of live registers); a compiler-only
-// fence every 4 rows bounds how far ahead they are issued.
+// to its start; a compiler-only fence per group of four rows bounds how far
+// ahead they are issued.
 #define NTK_TABLE_FENCE(k) \
   if (((k) & 3) == 3) asm volatile("" ::: "memory")
 
@@ -111,16 +120,19 @@ struct ChunkTabs {
 // reduce to one shuffle each (the plan checks the products on the host).
 template <int M, bool DECAY>
 __device__ __forceinline__ void chunk_solve(float (&v)[M], const ChunkTabs& t, unsigned lane) {
+  static_assert(M % 4 == 0, "rows per lane must be a multiple of 4");
   float yh = 0.f;
+  float4 L4;
 #pragma unroll
   for (int k = 0; k < M; ++k) {
-    yh = fmaf(-t.l[k], yh, v[k]);
+    if ((k & 3) == 0) L4 = t.q[5 * (k >> 2) + 0];
+    yh = fmaf(-comp4(L4, k & 3), yh, v[k]);
     v[k] = yh;
     NTK_TABLE_FENCE(k);
   }
   float B = yh;
   if (!DECAY) {
-    float A = t.gwp[M - 1].z;
+    float A = t.q[5 * (M / 4 - 1) + 3].w;  // phi of the chunk's last row
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const float Ap = __shfl_up_sync(FULL, A, d);
@@ -134,17 +146,22 @@ __device__ __forceinline__ void chunk_solve(float (&v)[M], const ChunkTabs& t, u
   float Yprev = __shfl_up_sync(FULL, B, 1);
   if (lane == 0) Yprev = 0.f;
   float xh = 0.f;
+  float4 G4, W4, P4;
 #pragma unroll
   for (int k = M - 1; k >= 0; --k) {
-    const float4 q = t.gwp[k];
-    const float y = fmaf(q.z, Yprev, v[k]);
-    xh = fmaf(-q.y, xh, q.x * y);
+    if ((k & 3) == 3) {
+      G4 = t.q[5 * (k >> 2) + 1];
+      W4 = t.q[5 * (k >> 2) + 2];
+      P4 = t.q[5 * (k >> 2) + 3];
+    }
+    const float y = fmaf(comp4(P4, k & 3), Yprev, v[k]);
+    xh = fmaf(-comp4(W4, k & 3), xh, comp4(G4, k & 3) * y);
     v[k] = xh;
-    NTK_TABLE_FENCE(k);
+    if ((k & 3) == 0) asm volatile("" ::: "memory");
   }
   float B2 = xh;
   if (!DECAY) {
-    float A2 = t.psi[0];
+    float A2 = t.q[4].x;  // psi of the chunk's first row
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const float Ap = __shfl_down_sync(FULL, A2, d);
@@ -157,9 +174,11 @@ __device__ __forceinline__ void chunk_solve(float (&v)[M], const ChunkTabs& t, u
   }
   float Xnext = __shfl_down_sync(FULL, B2, 1);
   if (lane == 31) Xnext = 0.f;
+  float4 S4;
 #pragma unroll
   for (int k = 0; k < M; ++k) {
-    v[k] = fmaf(t.psi[k], Xnext, v[k]);
+    if ((k & 3) == 0) S4 = t.q[5 * (k >> 2) + 4];
+    v[k] = fmaf(comp4(S4, k & 3), Xnext, v[k]);
     NTK_TABLE_FENCE(k);
   }
 }
@@ -204,17 +223,17 @@ struct RefineOcc {
 };
 
 // Shared-memory footprint of one CTA: two buffers of W padded system tiles,
-// the class tables (l and psi: 2 floats, gwp: a float4, per padded row)
+// the class tables (class_pitch4 float4s per class)
 // and, per buffer, the boundary stencils' inputs (3 doubles) and their
 // double-word results for rows 0 and n-1 of each system.
 #ifndef REFINE_GROUPS_PER_CTA
-#define REFINE_GROUPS_PER_CTA 2
+#define REFINE_GROUPS_PER_CTA 1
 #endif
 constexpr int kRefineBuffers = REFINE_GROUPS_PER_CTA > 1 ? 2 : 1;
 template <int M>
 __host__ __device__ constexpr size_t refine_smem(int W, int ncls) {
   return (((size_t)kRefineBuffers * W * sys_pitch<M>() * sizeof(double) + 15) & ~(size_t)15) +
-         (size_t)ncls * (M + 1) * (2 * sizeof(float) + sizeof(float4)) +
+         (size_t)ncls * class_pitch4<M>() * sizeof(float4) +
          (size_t)kRefineBuffers * 2 * W * (sizeof(float2) + 3 * sizeof(double));
 }
 
@@ -289,8 +308,7 @@ __device__ __forceinline__ void refine_system(double* trow, const float2* bndw, 
     for (int k = 0; k < M; ++k) {
       const double fnext = (k < M - 1) ? trow[cb + k + 1] : fright;
       float h, l;
-      split_f64(fnext - fprev, h, l, range);
-      fast_two_sum(h, l, h, l);
+      split_f64(fnext - fprev, h, l, range);  // h: D truncated to FP32, l: the next 23 bits
       x[k] = h;
       drow[cb + k] = make_float2(h, l);
       fprev = fcur;
@@ -317,8 +335,7 @@ __device__ __forceinline__ void refine_system(double* trow, const float2* bndw, 
 #pragma unroll
     for (int k = 0; k < M; ++k) {
       float h, l;
-      split_f64(trow[cb + k], h, l, range);
-      fast_two_sum(h, l, h, l);  // h = d rounded to FP32
+      split_f64(trow[cb + k], h, l, range);  // h: d truncated to FP32, l: the next 23 bits
       x[k] = h;
       drow[cb + k] = make_float2(h, l);
     }
@@ -570,15 +587,12 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
     refine_kernel(const double* in, double* out, int n, Batch b, RefineArgs ra) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int P = sys_pitch<M>();
-  constexpr int QSTEP = (32 / M) * (M + 1);  // tile_off(r + 32) - tile_off(r)
   const int W = blockDim.x >> 5;
-  const int TC = ra.ncls * (M + 1);  // table entries
+  const int TC = ra.ncls * class_pitch4<M>();  // table float4s
   double* tiles = reinterpret_cast<double*>(smem_raw);  // [buffers][W][P]
-  float4* tgwp = reinterpret_cast<float4*>(smem_raw + (((size_t)kRefineBuffers * W * P * sizeof(double) + 15) &
-                                                       ~(size_t)15));
-  float* tl_all = reinterpret_cast<float*>(tgwp + TC);
-  float* tpsi_all = tl_all + TC;
-  float2* bnd = reinterpret_cast<float2*>(tpsi_all + TC);              // [buffers][2W]: rows 0, n-1
+  float4* tq = reinterpret_cast<float4*>(smem_raw + (((size_t)kRefineBuffers * W * P * sizeof(double) + 15) &
+                                                     ~(size_t)15));
+  float2* bnd = reinterpret_cast<float2*>(tq + TC);                    // [buffers][2W]: rows 0, n-1
   double* braw = reinterpret_cast<double*>(bnd + kRefineBuffers * 2 * W);  // [buffers][2W][3]: stencil inputs
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
@@ -589,12 +603,10 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
   if (g >= ngroups) return;  // whole CTA
   unsigned range = 0;
 
-  const int cbase = __ldg(reinterpret_cast<const int*>(ra.tab) + lane) * (M + 1);
+  const int cbase = __ldg(reinterpret_cast<const int*>(ra.tab) + lane) * class_pitch4<M>();
   {
     const float4* g4 = reinterpret_cast<const float4*>(ra.tab + 32);
-    for (int i = tid; i < TC; i += blockDim.x) tgwp[i] = g4[i];
-    const float* lp = ra.tab + 32 + 4 * TC;
-    for (int i = tid; i < 2 * TC; i += blockDim.x) tl_all[i] = lp[i];
+    for (int i = tid; i < TC; i += blockDim.x) tq[i] = g4[i];
   }
 
   // The group sequence is unrolled at compile time: a run-time group loop
@@ -625,9 +637,7 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
     __syncthreads();  // group gc staged (all threads' copies), its bnd written
     if (warp < group_count(b, gc, W)) {
       ChunkTabs tabs;
-      tabs.l = tl_all + cbase;
-      tabs.gwp = tgwp + cbase;
-      tabs.psi = tpsi_all + cbase;
+      tabs.q = tq + cbase;
       refine_system<M, RHS, SWEEPS, POW2, PAD, DECAY>(tiles + ((size_t)buf * W + warp) * P,
                                                       bnd + (size_t)buf * 2 * W + 2 * warp, tabs, n, ra, lane, range);
     }

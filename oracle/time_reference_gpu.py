@@ -7,6 +7,10 @@ add the two permutes.  Prints one JSON line with ms per derivative and rows/s,
 the reference-kernel baseline for the 512^3 three-direction derivative.
 
     python oracle/time_reference_gpu.py [N] [reps]
+    python oracle/time_reference_gpu.py adi [N] [steps]
+
+The `adi` form times experiments/run-adi.py:59-71 instead (stencil, CR
+solve of rows 1..N-2, transpose, twice per step) on an N x N field.
 """
 import json
 import os
@@ -18,7 +22,59 @@ sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "near-toeplitz-applications_gb300"))
 
 
+def main_adi(N, steps):
+    import numpy as np
+    import torch
+
+    import oracle as O
+    from ntk.workloads import gaussians_2d
+
+    R = O.ref_gpu()
+    if R is None:
+        print(json.dumps({"unavailable": "reference kernels not built (oracle/_ref missing)"}))
+        return 0
+    dev = torch.device("cuda", 0)
+    dx = 1.0 / (N - 1)
+    dt = 2 * 0.5 * dx * dx  # r = 0.5
+    co = O.adi_coeffs(dx, dt)  # experiments/run-adi.py:50-53
+    u = gaussians_2d(N, seed=0, device=dev)
+    d_x = u.clone()
+    d_y = u.t().contiguous()
+    arrs = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in O.precompute(N, co)]
+    s = torch.cuda.current_stream().cuda_stream
+
+    def solve(x):  # rows 1..N-2, in place (experiments/run-adi.py:65)
+        assert R.ntkref_gpu_cr(N, N - 2, *[a.data_ptr() for a in arrs], co[0], co[1], co[2], co[3], co[4],
+                               x.data_ptr() + 8 * N, s) == 0
+
+    def step():
+        assert R.ntkref_gpu_adi_rhs(u.data_ptr(), d_x.data_ptr(), N, dx, dt, s) == 0
+        solve(d_x)
+        assert R.ntkref_gpu_transpose(d_x.data_ptr(), u.data_ptr(), N, s) == 0
+        assert R.ntkref_gpu_adi_rhs(u.data_ptr(), d_y.data_ptr(), N, dx, dt, s) == 0
+        solve(d_y)
+        assert R.ntkref_gpu_transpose(d_y.data_ptr(), u.data_ptr(), N, s) == 0
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    rows = 2 * (N - 2) * N
+    print(json.dumps({"workload": "reference kernels, ADI %d^2, r = 0.5" % N, "ms_per_step": ms,
+                      "rows_per_s": rows / (ms * 1e-3)}))
+    return 0
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "adi":
+        return main_adi(int(sys.argv[2]) if len(sys.argv) > 2 else 2048, int(sys.argv[3]) if len(sys.argv) > 3 else 20)
     import numpy as np
     import torch
 
