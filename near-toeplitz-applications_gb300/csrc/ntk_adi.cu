@@ -49,40 +49,6 @@ namespace {
 
 // Smallest halo H such that every forward window [gL-H, gL) and backward
 // window [(g+1)L, (g+1)L+H) has a factor product below 2^-64.
-SegParams choose_segments(const std::vector<double>& l, const std::vector<double>& w, int n, long long nsys) {
-  SegParams sp;
-  sp.P = 1;
-  sp.L = n;
-  sp.H = 0;
-  // enough threads to cover the GPU several times over
-  int P = 1;
-  while (nsys * P < 152LL * 96 && P < 64 && n / (2 * P) >= 64) P *= 2;
-  if (P == 1) return sp;
-  const int L = (n + P - 1) / P;
-  const double lim = std::ldexp(1.0, -64);
-  for (int H = 8; H <= L / 2; H += 2) {
-    bool ok = true;
-    for (int g = 1; g < P && ok; ++g) {
-      double prod = 1.0;
-      for (int i = std::max(1, g * L - H); i < g * L; ++i) prod *= std::fabs(l[i]);
-      ok = prod <= lim;
-    }
-    for (int g = 0; g < P - 1 && ok; ++g) {
-      double prod = 1.0;
-      const int e = std::min(n, (g + 1) * L);
-      for (int i = e; i < std::min(n, e + H); ++i) prod *= std::fabs(w[i - 1]);
-      ok = prod <= lim;
-    }
-    if (ok) {
-      sp.P = P;
-      sp.L = L;
-      sp.H = H;
-      return sp;
-    }
-  }
-  return sp;
-}
-
 }  // namespace
 
 int adi_step(Adi* a, double* u, double* d_x, const double* d_y, cudaStream_t st) {
@@ -163,7 +129,7 @@ int ntk_adi_create(ntk_adi** out, int N, double dx, double dt, int precision) {
   if (rc == NTK_OK) {
     std::vector<double> w(N);
     for (int i = 0; i < N; ++i) w[i] = (i < N - 1 ? a->plan.mat.c(i) : 0.0) / a->plan.lu_u[i];
-    a->sp = ntk::choose_segments(a->plan.lu_l, w, N, N - 2);
+    a->sp = ntk::choose_segments(a->plan.lu_l.data(), w.data(), N, N - 2);
     rc = ntk::cuda_status(cudaMalloc(&a->scratch, sizeof(double) * (size_t)N * N), "cudaMalloc(ADI scratch)");
   }
   if (rc) {

@@ -51,41 +51,6 @@ int scratch_address(int dev, double** out) {
   return NTK_OK;
 }
 
-// Same rule as the ADI plan: smallest halo whose windows' factor products
-// are below 2^-64, enough segments to cover the GPU; plain sweeps otherwise.
-SegParams static_segments(const double* l, const double* w, int n, long long nsys) {
-  SegParams sp;
-  sp.P = 1;
-  sp.L = n;
-  sp.H = 0;
-  int P = 1;
-  while (nsys * P < 152LL * 96 && P < 64 && n / (2 * P) >= 64) P *= 2;
-  if (P == 1) return sp;
-  const int L = (n + P - 1) / P;
-  const double lim = std::ldexp(1.0, -64);
-  for (int H = 8; H <= L / 2; H += 2) {
-    bool ok = true;
-    for (int g = 1; g < P && ok; ++g) {
-      double prod = 1.0;
-      for (int i = (g * L - H > 1 ? g * L - H : 1); i < g * L; ++i) prod *= std::fabs(l[i]);
-      ok = prod <= lim;
-    }
-    for (int g = 0; g < P - 1 && ok; ++g) {
-      double prod = 1.0;
-      const int e = ((g + 1) * L < n) ? (g + 1) * L : n;
-      for (int i = e; i < ((e + H < n) ? e + H : n); ++i) prod *= std::fabs(w[i - 1]);
-      ok = prod <= lim;
-    }
-    if (ok) {
-      sp.P = P;
-      sp.L = L;
-      sp.H = H;
-      return sp;
-    }
-  }
-  return sp;
-}
-
 }  // namespace
 }  // namespace ntk
 
@@ -142,7 +107,7 @@ extern "C" int ntk_adi_step_static(int N, double dx, double dt, double* u, doubl
     g[i] = 1.0 / ui;
     u_prev = ui;
   }
-  const SegParams sp = static_segments(l, w, N, N - 2);
+  const SegParams sp = choose_segments(l, w, N, N - 2);
 
   cudaStream_t st = (cudaStream_t)stream;
   double* dtab = scratch + (size_t)kMaxN * kMaxN;

@@ -1,6 +1,7 @@
 // ntk_internal.h -- host-side declarations shared by the ntk translation units.
 #pragma once
 #include <cuda_runtime.h>
+#include <cmath>
 #include <cstdint>
 #include <string>
 
@@ -55,6 +56,51 @@ struct SegParams {
   int H = 0;
   int P = 1;
 };
+
+// Segmentation of nsys systems of n rows for the segmented sweeps (the ADI
+// half-steps: few, long systems).  l[n], w[n]: the FP64 LU factors.  Aims
+// for ~16 warps per SM of (segment, system) threads and takes the largest
+// power-of-two P up to that for which some halo H <= L/2 makes every
+// truncated factor product (l over the H rows before a segment start, w over
+// the H rows after a segment end) fall below 2^-64, i.e. the truncation is
+// below FP64 rounding.  P = 1 (plain sweeps) when none qualifies.  Allocates
+// nothing.
+#ifndef NTK_SEG_THREADS
+#define NTK_SEG_THREADS (152 * 512)
+#endif
+inline SegParams choose_segments(const double* l, const double* w, int n, long long nsys) {
+  SegParams sp;
+  sp.P = 1;
+  sp.L = n;
+  sp.H = 0;
+  int Pmax = 1;
+  while (nsys * Pmax < (long long)NTK_SEG_THREADS && Pmax < 64 && n / (2 * Pmax) >= 16) Pmax *= 2;
+  const double lim = std::ldexp(1.0, -64);
+  for (int P = Pmax; P >= 2; P /= 2) {
+    const int L = (n + P - 1) / P;
+    for (int H = 8; H <= L / 2; H += 2) {
+      bool ok = true;
+      for (int g = 1; g < P && ok; ++g) {
+        double prod = 1.0;
+        for (int i = (g * L - H > 1 ? g * L - H : 1); i < g * L; ++i) prod *= std::fabs(l[i]);
+        ok = prod <= lim;
+      }
+      for (int g = 0; g < P - 1 && ok; ++g) {
+        double prod = 1.0;
+        const int e = ((g + 1) * L < n) ? (g + 1) * L : n;
+        for (int i = e; i < ((e + H < n) ? e + H : n); ++i) prod *= std::fabs(w[i - 1]);
+        ok = prod <= lim;
+      }
+      if (ok) {
+        sp.P = P;
+        sp.L = L;
+        sp.H = H;
+        return sp;
+      }
+    }
+  }
+  return sp;
+}
 
 // FP64 factor tables of the shared matrix (length n each), device memory.
 struct TablesF64 {
