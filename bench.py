@@ -464,40 +464,49 @@ def secondary_configs(dev, hbm):
     dx = 1.0 / (NA - 1)
     dt = 2 * 0.5 * dx * dx
     u0 = gaussians_2d(NA, seed=0, device=dev)
-    u, dxa, dya = u0.clone(), u0.clone(), u0.t().contiguous()
-    with ntk.Adi(NA, dx, dt) as adi:
-        adi.run(u, dxa, dya, steps, graph=True)  # capture + warm
-        torch.cuda.synchronize(dev)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        adi.run(u, dxa, dya, steps, graph=True)
-        e1.record()
-        torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1) / steps
-        # accuracy: 3 steps from u0 against the long-double Thomas pipeline
-        ug, xg, yg = u0.clone(), u0.clone(), u0.t().contiguous()
-        for _ in range(3):
-            adi.step(ug, xg, yg)
-        torch.cuda.synchronize(dev)
+    rows = 2 * (NA - 2) * NA
+    adi = {}
+    after3 = {}
+    for prec in ("fp64", "fp32_refine"):
+        u, dxa, dya = u0.clone(), u0.clone(), u0.t().contiguous()
+        with ntk.Adi(NA, dx, dt, precision=prec) as plan:
+            plan.run(u, dxa, dya, steps, graph=True)  # capture + warm
+            torch.cuda.synchronize(dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            plan.run(u, dxa, dya, steps, graph=True)
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ms = e0.elapsed_time(e1) / steps
+            # accuracy: 3 steps from u0
+            ug, xg, yg = u0.clone(), u0.clone(), u0.t().contiguous()
+            for _ in range(3):
+                plan.step(ug, xg, yg)
+            torch.cuda.synchronize(dev)
+            after3[prec] = ug.cpu().numpy()
+            seg = plan.segments
+        adi[prec] = {"ms_per_step": ms, "rows_per_s": rows / (ms * 1e-3),
+                     "hbm_frac": 32.0 * NA * NA / (ms * 1e-3) / 1e9 / hbm, "segments": seg}
+        del u, dxa, dya, ug, xg, yg
     ub = u0.cpu().numpy().copy()
     xb, yb = ub.copy(), ub.T.copy()
     for _ in range(3):
         O.adi_step_exact(ub, xb, yb, dx, dt)
-    err = O.rel_err(ug.cpu().numpy(), ub)
+    adi["fp64"]["rel_err_vs_oracle_3_steps"] = O.rel_err(after3["fp64"], ub)
+    adi["fp32_refine"]["rel_err_vs_oracle_3_steps"] = O.rel_err(after3["fp32_refine"], ub)
+    adi["fp32_refine"]["rel_err_vs_fp64_3_steps"] = O.rel_err(after3["fp32_refine"], after3["fp64"])
     uc = u0.cpu().numpy().copy()
     xc, yc = uc.copy(), uc.T.copy()
     t0 = time.perf_counter()
     O.adi_step_banded(uc, xc, yc, dx, dt)
     cpu_s = time.perf_counter() - t0
-    rows = 2 * (NA - 2) * NA
-    res["adi"] = {"workload": "ADI heat equation 2048^2, r = 0.5, %d steps as one CUDA graph" % steps,
-                  "precision": "fp64", "ms_per_step": ms, "rows_per_s": rows / (ms * 1e-3),
-                  "hbm_frac": 32.0 * NA * NA / (ms * 1e-3) / 1e9 / hbm,
-                  "rel_err_vs_oracle_3_steps": err,
-                  "cpu_baseline": {"rows_per_s": rows / cpu_s, "cores": 1, "kind": "port",
-                                   "sample": "one step, numpy stencil + scipy solve_banded per half step"}}
-    del u, dxa, dya, ug, xg, yg, u0
+    adi.update({"workload": "ADI heat equation 2048^2, r = 0.5, %d steps as one CUDA graph" % steps,
+                "speedup_refine_vs_fp64": adi["fp64"]["ms_per_step"] / adi["fp32_refine"]["ms_per_step"],
+                "cpu_baseline": {"rows_per_s": rows / cpu_s, "cores": 1, "kind": "port",
+                                 "sample": "one step, numpy stencil + scipy solve_banded per half step"}})
+    res["adi"] = adi
+    del u0
     # ---- uneven batch ----
     lengths, systems = uneven_batch(4096, 32, 8192, seed=0)
     interior = np.array([sy[0] for sy in systems])

@@ -22,6 +22,7 @@
 #include <tuple>
 #include <vector>
 
+#include "ntk_adi_refine.h"
 #include "ntk_internal.h"
 #include "ntk_plan.h"
 
@@ -35,6 +36,8 @@ struct Adi {
   double* scratch = nullptr;  // N x N forward values of the segmented sweeps
   SegParams sp;
   double bottom = 0, center = 0, top = 0;
+  AdiRefine* refine = nullptr;  // NTK_FP32 / NTK_FP32_REFINE half steps (ntk_adi_refine.cu)
+  int refine_w = 4;             // systems per CTA of the refinement windows
   cudaStream_t capture_stream = nullptr;
   std::map<std::tuple<const void*, const void*, const void*, int>, cudaGraphExec_t> graphs;
 
@@ -42,6 +45,7 @@ struct Adi {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     if (capture_stream) cudaStreamDestroy(capture_stream);
     if (scratch) cudaFree(scratch);
+    if (refine) adi_refine_destroy(refine);
   }
 };
 
@@ -52,6 +56,7 @@ namespace {
 }  // namespace
 
 int adi_step(Adi* a, double* u, double* d_x, const double* d_y, cudaStream_t st) {
+  if (a->refine) return adi_refine_step(a->refine, u, d_x, d_y, a->refine_w, st);
   const int N = a->N;
   TablesF64 t;
   t.l = a->plan.d_lw;
@@ -107,9 +112,9 @@ int ntk_adi_create(ntk_adi** out, int N, double dx, double dt, int precision) {
     ntk::set_error("ntk_adi_create: need N >= 4 and positive finite dx, dt");
     return NTK_ERR_INVALID;
   }
-  if (precision != NTK_FP64) {
-    ntk::set_error("ntk_adi_create: this build runs ADI in NTK_FP64 only");
-    return NTK_ERR_UNSUPPORTED;
+  if (precision != NTK_FP64 && precision != NTK_FP32 && precision != NTK_FP32_REFINE) {
+    ntk::set_error("ntk_adi_create: unknown precision %d", precision);
+    return NTK_ERR_INVALID;
   }
   ntk_adi* a = new (std::nothrow) ntk_adi();
   if (!a) {
@@ -130,7 +135,10 @@ int ntk_adi_create(ntk_adi** out, int N, double dx, double dt, int precision) {
     std::vector<double> w(N);
     for (int i = 0; i < N; ++i) w[i] = (i < N - 1 ? a->plan.mat.c(i) : 0.0) / a->plan.lu_u[i];
     a->sp = ntk::choose_segments(a->plan.lu_l.data(), w.data(), N, N - 2);
-    rc = ntk::cuda_status(cudaMalloc(&a->scratch, sizeof(double) * (size_t)N * N), "cudaMalloc(ADI scratch)");
+    if (precision == NTK_FP64)
+      rc = ntk::cuda_status(cudaMalloc(&a->scratch, sizeof(double) * (size_t)N * N), "cudaMalloc(ADI scratch)");
+    else
+      rc = ntk::adi_refine_create(&a->refine, N, dx, dt, precision);
   }
   if (rc) {
     delete a;
@@ -149,6 +157,15 @@ int ntk_adi_segments(const ntk_adi* adi, int* seg_len, int* halo, int* nseg) {
   if (!adi) {
     ntk::set_error("ntk_adi_segments: null plan");
     return NTK_ERR_INVALID;
+  }
+  if (adi->refine) {
+    // refinement windows: central rows per window, halo, windows per system
+    int L = 0, H = 0, P = 0;
+    ntk::adi_refine_windows(adi->refine, &L, &H, &P);
+    if (seg_len) *seg_len = L;
+    if (halo) *halo = H;
+    if (nseg) *nseg = P;
+    return NTK_OK;
   }
   if (seg_len) *seg_len = adi->sp.L;
   if (halo) *halo = adi->sp.H;

@@ -1,0 +1,361 @@
+// ntk_adi_refine.cu -- ADI half-steps (experiments/run-adi.py:59-71) with
+// the FP32 solve + double-word refinement of ntk_refine.cuh.
+//
+// A half-step solves N-2 systems of N rows (2046 x 2048 at the benchmark
+// size), too long for one warp's registers.  Each system is cut into
+// windows of Lw = 32 M rows that overlap by halos of H rows: window g
+// writes back only its central rows, and every row it writes is at least
+// H rows from a cut end.  The refinement converges to the exact solution of
+// the window's own (truncated) system, so the truncation itself must lie
+// below the target accuracy: H is chosen so that the product of the LU
+// multipliers over H rows is below 2^-56 (r = 0.5: |l| -> 0.268, H = 32).
+// Four window kinds have their own matrices and FP32 tables:
+//   first : row 0 is the system's identity row, row Lw-1 is cut (c = 0)
+//   middle: both ends cut (row 0 has a = 0, row Lw-1 has c = 0)
+//   last  : row 0 cut, row Lw-1 is the system's identity row
+//   whole : N == Lw, both identity rows, no truncation.
+//
+// The rows are scaled by dx^2, so the interior matrix is (1, beta, 1) with
+// beta = -2 (1 + dx^2/dt) (= -4 at r = 0.5: all powers of two, exact
+// residual products) and the right-hand side of the vertical stencil
+// (adi/rhs.py:21-24) becomes  d = gamma * u_mid - (u_lo + u_hi),
+// gamma = 2 (1 - dx^2/dt): one or two FP64 instructions per row, the only
+// FP64 work.  A CTA takes W consecutive systems of one window and stages
+// the W + 2 lines their stencils read with cp.async.
+#include <cmath>
+#include <vector>
+
+#include "ntk_adi_refine.h"
+#include "ntk_refine.cuh"
+
+namespace ntk {
+
+struct AdiWin {
+  int out_lo = 0, out_hi = 0;  // window rows written back
+  int head_bnd = 0;            // window row 0 is the system's identity row 0
+  int tail_bnd = 0;            // window row Lw-1 is the system's identity row N-1
+  double gamma = 0.0;          // d = gamma * mid - (lo + hi)
+  const double* bnd = nullptr; // identity-row right-hand sides: system s, system row i at
+  long long bnd_ss = 0;        //   bnd[s * bnd_ss + i * bnd_es]
+  long long bnd_es = 0;
+  int n_sys = 0;               // system length N
+};
+
+namespace refine_detail {
+
+template <int M>
+__host__ __device__ constexpr size_t adi_smem(int W, int ncls) {
+  // line buffer (W + 2 lines) and W system tiles, padded chunk layout, + tables
+  return (size_t)(2 * W + 2) * sys_pitch<M>() * sizeof(double) + 8 +
+         (size_t)ncls * class_pitch4<M>() * sizeof(float4);
+}
+
+// b: nsys = systems x windows of this launch, ni = systems, is = line
+// stride, os = distance between consecutive windows, es = element stride;
+// in/out point at window row 0 of the launch's first window of system 0.
+// The CTA's W systems are consecutive systems of one window.
+template <int M, int SWEEPS, bool POW2, bool DECAY>
+__global__ void __launch_bounds__(256, RefineOcc<M>::value)
+    adi_refine_kernel(const double* in, double* out, Batch b, AdiWin aw, RefineArgs ra) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int P = sys_pitch<M>();
+  constexpr int LW = 32 * M;
+  const int W = blockDim.x >> 5;
+  const int TC = ra.ncls * class_pitch4<M>();
+  double* lines = reinterpret_cast<double*>(smem_raw);  // [W + 2][P]
+  double* tiles = lines + (size_t)(W + 2) * P;           // [W][P]
+  float4* tq = reinterpret_cast<float4*>(smem_raw + (((size_t)(2 * W + 2) * P * sizeof(double) + 15) & ~(size_t)15));
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const unsigned lane = tid & 31;
+  const long long nsysw = b.ni;                          // systems per window
+  const long long nblk = (nsysw + W - 1) / W;            // CTAs per window
+  const long long win = blockIdx.x / nblk;
+  const long long s0 = (blockIdx.x % nblk) * W;          // first system of the CTA
+  const int wc = (int)((nsysw - s0) < W ? (nsysw - s0) : W);
+  unsigned range = 0;
+
+  const int cbase = __ldg(reinterpret_cast<const int*>(ra.tab) + lane) * class_pitch4<M>();
+  {
+    const float4* g4 = reinterpret_cast<const float4*>(ra.tab + 32);
+    for (int i = tid; i < TC; i += blockDim.x) tq[i] = g4[i];
+  }
+
+  // ---- stage lines s0-1 .. s0+wc (the stencil's neighbours included) ----
+  // Line j of the buffer is system line s0 - 1 + j; lanes walk rows for
+  // unit element stride (256-byte rows of copies), lines otherwise.
+  const double* wbase = in + win * b.os;
+  const int nl = wc + 2;
+  const int total = nl * LW;
+  for (int idx = tid; idx < total; idx += blockDim.x) {
+    int j, r;
+    if (b.es == 1) {
+      j = idx / LW;
+      r = idx - j * LW;
+    } else {
+      r = idx / nl;
+      j = idx - r * nl;
+    }
+    const double* src = wbase + (s0 - 1 + j) * b.is + (long long)r * b.es;
+    cp_async8(lines + (size_t)j * P + tile_off<M>(r), src, 8u);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+
+  if (warp < wc) {
+    // ---- double-word right-hand side into this system's tile ----
+    const int cb = (int)lane * (M + 1);
+    const double* lo = lines + (size_t)warp * P;
+    const double* mid = lo + P;
+    const double* hi = mid + P;
+    double* trow = tiles + (size_t)warp * P;
+    float2* drow = reinterpret_cast<float2*>(trow);
+    const long long s = s0 + warp;
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      double d = -(lo[cb + k] + hi[cb + k]);
+      if (aw.gamma != 0.0) d = fma(aw.gamma, mid[cb + k], d);
+      float h, l;
+      split_f64(d, h, l, range);
+      drow[cb + k] = make_float2(h, l);
+    }
+    // identity rows: x = the boundary value (adi/rhs.py leaves them to the
+    // solve's first and last rows, experiments/run-adi.py:50-53)
+    if (aw.head_bnd && lane == 0) {
+      float h, l;
+      split_f64(aw.bnd[s * aw.bnd_ss], h, l, range);
+      drow[0] = make_float2(h, l);
+    }
+    if (aw.tail_bnd && lane == 31) {
+      float h, l;
+      split_f64(aw.bnd[s * aw.bnd_ss + (long long)(aw.n_sys - 1) * aw.bnd_es], h, l, range);
+      drow[tile_off<M>(LW - 1)] = make_float2(h, l);
+    }
+    __syncwarp();
+    ChunkTabs tabs;
+    tabs.q = tq + cbase;
+    refine_system<M, RHS_PRESPLIT, SWEEPS, POW2, false, DECAY>(trow, nullptr, tabs, LW, ra, lane, range);
+    __syncwarp();
+    // ---- write back the window's central rows (coalesced for unit stride) ----
+    double* dst = out + win * b.os + s * b.is;
+#pragma unroll 4
+    for (int q = 0; q < M; ++q) {
+      const int r = (int)lane + 32 * q;
+      if (r >= aw.out_lo && r < aw.out_hi) dst[(long long)r * b.es] = trow[tile_off<M>(r)];
+    }
+  }
+  if (range && ra.status) atomicOr(ra.status, 1u);
+}
+
+template <int M, int SWEEPS, bool POW2, bool DECAY>
+int adi_launch(const double* in, double* out, const Batch& b, const AdiWin& aw, const RefineArgs& ra, int W,
+               cudaStream_t st) {
+  const size_t smem = adi_smem<M>(W, ra.ncls);
+  auto kern = adi_refine_kernel<M, SWEEPS, POW2, DECAY>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(adi_refine_kernel)");
+  const long long windows = b.nsys / b.ni;
+  const long long blocks = windows * ((b.ni + W - 1) / W);
+  if (blocks <= 0) return NTK_OK;
+  if (blocks > 0x7fffffffLL) {
+    set_error("too many ADI windows for one launch");
+    return NTK_ERR_INVALID;
+  }
+  kern<<<(unsigned)blocks, W * 32, smem, st>>>(in, out, b, aw, ra);
+  return cuda_status(cudaGetLastError(), "adi_refine_kernel");
+}
+
+template <int M, bool DECAY>
+int adi_dispatch(const double* in, double* out, const Batch& b, const AdiWin& aw, const RefineArgs& ra, bool pow2,
+                 int sweeps, int W, cudaStream_t st) {
+  if (sweeps == 0)
+    return pow2 ? adi_launch<M, 0, true, DECAY>(in, out, b, aw, ra, W, st)
+                : adi_launch<M, 0, false, DECAY>(in, out, b, aw, ra, W, st);
+  if (sweeps == 1)
+    return pow2 ? adi_launch<M, 1, true, DECAY>(in, out, b, aw, ra, W, st)
+                : adi_launch<M, 1, false, DECAY>(in, out, b, aw, ra, W, st);
+  return pow2 ? adi_launch<M, 2, true, DECAY>(in, out, b, aw, ra, W, st)
+              : adi_launch<M, 2, false, DECAY>(in, out, b, aw, ra, W, st);
+}
+
+}  // namespace refine_detail
+
+struct AdiRefine {
+  int N = 0;
+  int M = 0, Lw = 0, H = 0, L = 0, P = 0;  // rows per lane, window, halo, central rows, windows
+  int sweeps = 1;
+  double gamma = 0.0;
+  bool whole = false;  // N == Lw: one window per system, no truncation
+  Plan win[4];         // first, middle, last, whole window matrices (n = Lw)
+};
+
+int adi_refine_create(AdiRefine** out, int N, double dx, double dt, int precision) {
+  *out = nullptr;
+  AdiRefine* ar = new (std::nothrow) AdiRefine();
+  if (!ar) {
+    set_error("out of host memory");
+    return NTK_ERR_ALLOC;
+  }
+  ar->N = N;
+  ar->sweeps = (precision == NTK_FP32) ? 0 : 1;
+  const double q = dx * dx / dt;
+  const double beta = -2.0 * (1.0 + q);
+  ar->gamma = 2.0 * (1.0 - q);
+  // window length: the largest 32 M <= N with M in {16, 8, 4}
+  for (int m : {16, 8, 4})
+    if (32 * m <= N) {
+      ar->M = m;
+      break;
+    }
+  if (ar->M == 0) {
+    set_error("ADI in FP32/FP32+refine needs N >= 128 (got %d); use NTK_FP64", N);
+    delete ar;
+    return NTK_ERR_UNSUPPORTED;
+  }
+  ar->Lw = 32 * ar->M;
+  // halo: rows until the product of the LU multipliers of a window cut
+  // (|l_i| = |1/u_{i-1}|, starting from u = beta at the cut; |w_i| = |1/u_i|
+  // is the same sequence one row on) falls below 2^-56, plus two
+  double linf = 0.0;
+  {
+    const double lim = std::ldexp(1.0, -56);
+    double u = beta, prod = 1.0;
+    int H = 0;
+    while (prod > lim && H < 4 * ar->Lw) {
+      const double l = 1.0 / u;
+      prod *= std::fabs(l);
+      u = beta - l;
+      linf = std::fabs(l);
+      ++H;
+    }
+    ar->H = (H + 2 + 1) & ~1;
+  }
+  // a slowly decaying LU (|l| -> above 1/2) belongs to a badly conditioned
+  // matrix (r = 40: |l| -> 0.85): one sweep then leaves ~1e-12, a second one
+  // restores ~1e-14
+  if (ar->sweeps > 0 && linf > 0.5) ar->sweeps = 2;
+  ar->whole = (N == ar->Lw);
+  ar->L = ar->whole ? ar->Lw : ar->Lw - 2 * ar->H;
+  if (!ar->whole && ar->L < ar->Lw / 4) {
+    set_error("ADI in FP32/FP32+refine: the factors decay too slowly for %d-row windows (halo %d); use NTK_FP64",
+              ar->Lw, ar->H);
+    delete ar;
+    return NTK_ERR_UNSUPPORTED;
+  }
+  // windows: first [0, Lw) writes [0, L); middle g writes [gL, gL + L) from
+  // [gL - H, gL + L + H); last [N - Lw, N) writes [(P-1) L, N)
+  const int Pm1 = (N - ar->Lw + ar->H + ar->L - 1) / ar->L;  // ceil((N - Lw + H) / L)
+  ar->P = ar->whole ? 1 : (Pm1 < 1 ? 1 : Pm1) + 1;
+  // scaled rows: coeffs (b1, c1, ai, bi, ci, an, bn)
+  const double first[7] = {1.0, 0.0, 1.0, beta, 1.0, 1.0, beta};
+  const double middle[7] = {beta, 1.0, 1.0, beta, 1.0, 1.0, beta};
+  const double last[7] = {beta, 1.0, 1.0, beta, 1.0, 0.0, 1.0};
+  const double whole[7] = {1.0, 0.0, 1.0, beta, 1.0, 0.0, 1.0};
+  const double* co[4] = {first, middle, last, whole};
+  for (int k = 0; k < 4; ++k) {
+    if ((k == 3) != ar->whole) continue;
+    int rc = ar->win[k].init(ar->Lw, 1, co[k], NTK_FP32_REFINE, 1);
+    if (rc == NTK_OK) rc = ar->win[k].init_refine();
+    if (rc) {
+      delete ar;
+      return rc;
+    }
+  }
+  *out = ar;
+  return NTK_OK;
+}
+
+void adi_refine_destroy(AdiRefine* ar) { delete ar; }
+
+void adi_refine_windows(const AdiRefine* ar, int* L, int* H, int* P) {
+  *L = ar->L;
+  *H = ar->whole ? 0 : ar->H;
+  *P = ar->P;
+}
+
+namespace {
+
+int run_windows(AdiRefine* ar, int kind, const double* in, double* out, Batch b, AdiWin aw, int W, cudaStream_t st) {
+  RefineArgs ra;
+  int M = 0;
+  bool p2 = false, dec = false;
+  int rc = refine_args(ar->win[kind], 1.0, 1.0, 1.0, &ra, &M, &p2, &dec);
+  if (rc) return rc;
+  using namespace refine_detail;
+  switch (M) {
+    case 4: return adi_dispatch<4, false>(in, out, b, aw, ra, p2, ar->sweeps, W, st);
+    case 8: return adi_dispatch<8, false>(in, out, b, aw, ra, p2, ar->sweeps, W, st);
+    default:
+      return dec ? adi_dispatch<16, true>(in, out, b, aw, ra, p2, ar->sweeps, W, st)
+                 : adi_dispatch<16, false>(in, out, b, aw, ra, p2, ar->sweeps, W, st);
+  }
+}
+
+// One half step: systems s = 0..N-3 are lines s+1 of the field; in/out point
+// at system 0's row 0; `is` is the line stride, `es` the row stride.
+int half_step(AdiRefine* ar, const double* in, double* out, long long is, long long es, const double* bnd,
+              long long bnd_ss, long long bnd_es, int W, cudaStream_t st) {
+  const int N = ar->N, Lw = ar->Lw, H = ar->H, L = ar->L, P = ar->P;
+  AdiWin aw;
+  aw.gamma = ar->gamma;
+  aw.bnd = bnd;
+  aw.bnd_ss = bnd_ss;
+  aw.bnd_es = bnd_es;
+  aw.n_sys = N;
+  Batch b;
+  b.ni = N - 2;
+  b.is = is;
+  b.es = es;
+  if (ar->whole) {
+    b.nsys = b.ni;
+    b.os = 0;
+    aw.out_lo = 0;
+    aw.out_hi = Lw;
+    aw.head_bnd = 1;
+    aw.tail_bnd = 1;
+    return run_windows(ar, 3, in, out, b, aw, W, st);
+  }
+  // first windows
+  b.nsys = b.ni;
+  b.os = 0;
+  aw.out_lo = 0;
+  aw.out_hi = L;
+  aw.head_bnd = 1;
+  aw.tail_bnd = 0;
+  int rc = run_windows(ar, 0, in, out, b, aw, W, st);
+  if (rc) return rc;
+  // middle windows g = 1 .. P-2 (window start gL - H)
+  if (P > 2) {
+    b.nsys = b.ni * (P - 2);
+    b.os = (long long)L * es;
+    aw.out_lo = H;
+    aw.out_hi = H + L;
+    aw.head_bnd = 0;
+    aw.tail_bnd = 0;
+    const long long off = (long long)(L - H) * es;
+    rc = run_windows(ar, 1, in + off, out + off, b, aw, W, st);
+    if (rc) return rc;
+  }
+  // last windows: [N - Lw, N), writing rows (P-1) L .. N-1
+  b.nsys = b.ni;
+  b.os = 0;
+  aw.out_lo = (P - 1) * L - (N - Lw);
+  aw.out_hi = Lw;
+  aw.head_bnd = 0;
+  aw.tail_bnd = 1;
+  const long long off = (long long)(N - Lw) * es;
+  return run_windows(ar, 2, in + off, out + off, b, aw, W, st);
+}
+
+}  // namespace
+
+int adi_refine_step(AdiRefine* ar, double* u, double* d_x, const double* d_y, int W, cudaStream_t st) {
+  const int N = ar->N;
+  // x half: systems = rows 1..N-2, stencil of u's rows, boundary RHS from d_x
+  int rc = half_step(ar, u + N, d_x + N, N, 1, d_x + N, N, 1, W, st);
+  if (rc) return rc;
+  // y half: systems = columns 1..N-2 of d_x, result into u, boundary RHS from d_y
+  return half_step(ar, d_x + 1, u + 1, 1, N, d_y + N, N, 1, W, st);
+}
+
+}  // namespace ntk

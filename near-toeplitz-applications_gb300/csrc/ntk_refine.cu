@@ -176,8 +176,36 @@ int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsPar
     return NTK_ERR_INVALID;
   }
   RefineArgs ra;
-  ra.tab = refine->d_tab;
-  ra.ncls = refine->ncls;
+  int M = 0;
+  bool p2 = false, d = false;
+  int rc = refine_args(*this, rp.sigma0, rp.sigmaN, s, &ra, &M, &p2, &d);
+  if (rc) return rc;
+  const int W = tune_refine_w;
+  const int sweeps_eff = (precision == NTK_FP32) ? 0 : sweeps;
+  switch (M) {
+    case 4: return refine_dispatch<4, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+    case 8: return refine_dispatch<8, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+    case 16:
+      return d ? refine_dispatch<16, true>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream)
+               : refine_dispatch<16, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+    default:
+      return d ? refine_dispatch<32, true>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream)
+               : refine_dispatch<32, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+  }
+}
+
+int refine_args(const Plan& p, double sigma0, double sigmaN, double s, RefineArgs* out, int* Mout, bool* pow2,
+                bool* decay) {
+  const RefineState* st = p.refine;
+  if (!st || !st->d_tab) {
+    set_error("plan has no FP32 tables");
+    return NTK_ERR_INVALID;
+  }
+  const Matrix& mat = p.mat;
+  const int n = p.n;
+  RefineArgs ra;
+  ra.tab = st->d_tab;
+  ra.ncls = st->ncls;
   ra.ai = to_dw(mat.ai);
   ra.bi = to_dw(mat.bi);
   ra.ci = to_dw(mat.ci);
@@ -193,25 +221,16 @@ int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsPar
     ra.td[i][1] = to_dw(tr >= 0 && tr < n ? mat.b(tr) : 1.0);
     ra.td[i][2] = to_dw(tr >= 0 && tr < n - 1 ? mat.c(tr) : 0.0);
   }
-  ra.sigma0 = rp.sigma0;
-  ra.sigmaN = rp.sigmaN;
+  ra.sigma0 = sigma0;
+  ra.sigmaN = sigmaN;
   ra.s = to_dw(s);
   ra.unit_scale = (s == 1.0) ? 1 : 0;
-  ra.status = refine->d_status;
-  const int W = tune_refine_w;
-  const int sweeps_eff = (precision == NTK_FP32) ? 0 : sweeps;
-  const bool d = refine->decay;
-  const bool p2 = refine->pow2;
-  switch (refine->M) {
-    case 4: return refine_dispatch<4, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
-    case 8: return refine_dispatch<8, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
-    case 16:
-      return d ? refine_dispatch<16, true>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream)
-               : refine_dispatch<16, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
-    default:
-      return d ? refine_dispatch<32, true>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream)
-               : refine_dispatch<32, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
-  }
+  ra.status = st->d_status;
+  *out = ra;
+  *Mout = st->M;
+  *pow2 = st->pow2;
+  *decay = st->decay;
+  return NTK_OK;
 }
 
 }  // namespace ntk

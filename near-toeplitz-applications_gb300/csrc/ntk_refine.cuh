@@ -72,6 +72,17 @@ template <int M, bool DECAY>
 int refine_dispatch(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2,
                     int sweeps, int rhs, int W, cudaStream_t st);
 
+// The plan's FP32 state for callers outside ntk_refine.cu (the ADI windows):
+// kernel arguments for right-hand-side scales sigma0/sigmaN and output scale
+// s, and the kernel shape (rows per lane, power-of-two interior, one-shuffle
+// carries).
+int refine_args(const Plan& p, double sigma0, double sigmaN, double s, RefineArgs* ra, int* M, bool* pow2,
+                bool* decay);
+
+// RHS kind of refine_system for tiles that already hold the double-word RHS
+// (hi, lo) in their slots (the ADI windows form their stencil themselves).
+constexpr int RHS_PRESPLIT = 100;
+
 namespace refine_detail {
 
 constexpr unsigned FULL = 0xffffffffu;
@@ -331,6 +342,9 @@ __device__ __forceinline__ void refine_system(double* trow, const float2* bndw, 
       }
       drow[tile_off<M>(n1)] = d1;
     }
+  } else if (RHS == RHS_PRESPLIT) {
+#pragma unroll
+    for (int k = 0; k < M; ++k) x[k] = drow[cb + k].x;
   } else {
 #pragma unroll
     for (int k = 0; k < M; ++k) {
