@@ -185,7 +185,10 @@ int ntk_adi_step_static(int N, double dx, double dt, double* u, double* d_x, con
 typedef struct ntk_batch ntk_batch;
 
 /* Factors every system on the host (FP64) and uploads the tables; allocates
- * a work array as large as the data buffer.  precision: NTK_FP64.
+ * a work array as large as the data buffer.  precision: NTK_FP64, or
+ * NTK_FP32_REFINE / NTK_FP32: systems cut into overlapping 512-row windows
+ * solved in FP32 with one double-word refinement sweep (NTK_ERR_UNSUPPORTED
+ * when some system's pivots decay too slowly, |a/u|, |c/u| >= 0.75).
  * Synchronous. */
 int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long long* offset, const double* interior,
                      const double* head, const double* tail, int precision);

@@ -29,6 +29,7 @@
 #include <numeric>
 #include <vector>
 
+#include "ntk_batch_refine.h"
 #include "ntk_internal.h"
 #include "ntk_plan.h"
 
@@ -124,8 +125,10 @@ struct Batch_ {
   int grid = 0;
   long long max_n = 0;
   long long segmented = 0;
+  BatchRefine* refine = nullptr;  // NTK_FP32 / NTK_FP32_REFINE windows (ntk_batch_refine.cu)
 
   ~Batch_() {
+    if (refine) batch_refine_destroy(refine);
     if (d_desc) cudaFree(d_desc);
     if (d_order) cudaFree(d_order);
     if (d_pool) cudaFree(d_pool);
@@ -248,9 +251,9 @@ int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long l
     return NTK_ERR_INVALID;
   }
   *out = nullptr;
-  if (precision != NTK_FP64) {
-    ntk::set_error("ntk_batch_create: this build solves uneven batches in NTK_FP64 only");
-    return NTK_ERR_UNSUPPORTED;
+  if (precision != NTK_FP64 && precision != NTK_FP32 && precision != NTK_FP32_REFINE) {
+    ntk::set_error("ntk_batch_create: unknown precision %d", precision);
+    return NTK_ERR_INVALID;
   }
   if (nsys > 0x7fffffffLL) {
     ntk::set_error("ntk_batch_create: too many systems");
@@ -328,6 +331,8 @@ int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long l
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
     b->grid = sms * 8;  // 8 CTAs of 4 warps per SM, persistent
+    if (!rc && precision != NTK_FP64)
+      rc = ntk::batch_refine_create(&b->refine, nsys, n, offset, interior, head, tail, precision);
   }
   if (rc) {
     delete b;
@@ -365,6 +370,7 @@ int ntk_batch_solve(ntk_batch* b, double* d, void* stream) {
     return NTK_ERR_INVALID;
   }
   cudaStream_t st = (cudaStream_t)stream;
+  if (b->refine) return ntk::batch_refine_solve(b->refine, d, b->d_scratch, b->total, st);
   int rc = ntk::cuda_status(cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), st), "cudaMemsetAsync(counter)");
   if (rc) return rc;
   ntk::batch_f64_kernel<<<b->grid, 128, 0, st>>>(d, b->d_scratch, b->d_desc, b->d_order, b->nsys, b->d_pool,

@@ -1,0 +1,388 @@
+// ntk_batch_refine.cu -- uneven batches in FP32 + double-word refinement.
+//
+// Same windows as the ADI path (ntk_adi_refine.cu): a system longer than
+// Lw = 512 rows is cut into windows overlapping by H-row halos (H: LU
+// multiplier products below 2^-56 for the slowest-decaying system), each
+// solved by one warp with the refine kernel's machinery (refine_system) and
+// writing back only its central rows; a shorter system is one window padded
+// with identity rows.  Every system has its own coefficients, so each warp
+// builds its window's FP32 factor tables itself, lane-parallel: lane j runs
+// the pivot recurrence over its 16 rows starting from the system's converged
+// pivot carried through the two rows before its chunk (lane 0 from the
+// window's exact first row).  For these near-Toeplitz
+// matrices the pivots reach the fixed point within a few rows (the transient
+// shrinks by ~(a c / u^2) per row), so the tables are the window's FP32 LU;
+// they only precondition the refinement, whose residual uses the exact
+// double-word rows.  Windows overlap, so the batch copies d to its work
+// array first and the windows read from there and write d.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ntk_batch_refine.h"
+#include "ntk_refine.cuh"
+
+namespace ntk {
+
+// One window: rows [r0, r0 + nwin) of a system; written back: window rows
+// [out_lo, out_hi).  Row coefficients as refine_system reads them.
+struct BatchWin {
+  long long off = 0;  // element offset of window row 0 in d
+  int nwin = 0;
+  int out_lo = 0, out_hi = 0;
+  int nh = 1, nt = 1;  // special rows at the window's head / tail
+  float uinf = 1.f;    // the system's converged pivot (FP32)
+  DW ai, bi, ci;
+  DW hd[2][3];
+  DW td[2][3];
+  DW s;                // output scale (1)
+  int unit_scale = 1;
+  int pad_ = 0;
+};
+
+namespace refine_detail {
+
+constexpr int BM = 16;                  // rows per lane
+constexpr int BLW = 32 * BM;            // window rows
+constexpr int BW = 4;                   // warps (windows) per CTA
+constexpr int BTAB = 32 * class_pitch4<BM>();  // float4s of one warp's tables
+
+__device__ __forceinline__ void row_coeffs(const BatchWin& w, int r, float& a, float& b, float& c) {
+  if (r >= w.nwin) {
+    a = 0.f;
+    b = 1.f;
+    c = 0.f;
+  } else if (r < w.nh) {
+    a = w.hd[r][0].h;
+    b = w.hd[r][1].h;
+    c = w.hd[r][2].h;
+  } else if (r >= w.nwin - w.nt) {
+    const int q = r - (w.nwin - w.nt);
+    a = w.td[q][0].h;
+    b = w.td[q][1].h;
+    c = w.td[q][2].h;
+  } else {
+    a = w.ai.h;
+    b = w.bi.h;
+    c = w.ci.h;
+  }
+}
+
+template <int SWEEPS, bool PAD>
+__global__ void __launch_bounds__(32 * BW) batch_refine_kernel(const double* __restrict__ src, double* dst,
+                                                               const BatchWin* __restrict__ wins, int nwins,
+                                                               unsigned* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int P = sys_pitch<BM>();
+  const int warp = threadIdx.x >> 5;
+  const unsigned lane = threadIdx.x & 31;
+  float4* tq = reinterpret_cast<float4*>(smem_raw) + (size_t)warp * BTAB;
+  BatchWin* wa = reinterpret_cast<BatchWin*>(reinterpret_cast<float4*>(smem_raw) + (size_t)BW * BTAB) + warp;
+  double* trow = reinterpret_cast<double*>(reinterpret_cast<BatchWin*>(reinterpret_cast<float4*>(smem_raw) +
+                                                                        (size_t)BW * BTAB) + BW) + (size_t)warp * P;
+  const long long item = (long long)blockIdx.x * BW + warp;
+  if (item >= nwins) return;  // whole warp; no CTA barriers below
+  unsigned range = 0;
+
+  // window descriptor into shared memory
+  {
+    const int* g = reinterpret_cast<const int*>(wins + item);
+    int* sdst = reinterpret_cast<int*>(wa);
+    constexpr int NW = (int)(sizeof(BatchWin) / sizeof(int));
+    for (int i = lane; i < NW; i += 32) sdst[i] = __ldg(g + i);
+  }
+  __syncwarp();
+  const BatchWin& w = *wa;
+  // stage the window (rows lane + 32q; zero beyond nwin)
+  {
+    const double* gsrc = src + w.off;
+#pragma unroll
+    for (int q = 0; q < BM; ++q) {
+      const int r = (int)lane + 32 * q;
+      const bool ok = !PAD || r < w.nwin;
+      cp_async8(trow + tile_off<BM>(r), ok ? gsrc + r : src, ok ? 8u : 0u);
+    }
+  }
+  // FP32 factor tables of this lane's 16 rows (layout of ChunkTabs)
+  {
+    const int r0 = (int)lane * BM;
+    float l[BM], g[BM], wv[BM];
+    float a, b, c, cprev;
+    float u;
+    if (lane == 0) {
+      u = 0.f;
+      cprev = 0.f;
+    } else {
+      // incoming pivot: the converged one, carried through the two rows
+      // before the chunk (they may be the system's special tail rows)
+      float ap, bp;
+      row_coeffs(w, r0 - 3, ap, bp, cprev);
+      u = w.uinf;
+#pragma unroll
+      for (int r = r0 - 2; r < r0; ++r) {
+        row_coeffs(w, r, a, b, c);
+        u = b - (a / u) * cprev;
+        cprev = c;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < BM; ++k) {
+      row_coeffs(w, r0 + k, a, b, c);
+      const float lk = (r0 + k == 0) ? 0.f : a / u;
+      u = b - lk * cprev;
+      l[k] = lk;
+      g[k] = 1.f / u;
+      wv[k] = c * g[k];
+      cprev = c;
+    }
+    float phi = 1.f, psi = 1.f;
+    float ph[BM], ps[BM];
+#pragma unroll
+    for (int k = 0; k < BM; ++k) {
+      phi *= -l[k];
+      ph[k] = phi;
+    }
+#pragma unroll
+    for (int k = BM - 1; k >= 0; --k) {
+      psi *= -wv[k];
+      ps[k] = psi;
+    }
+    float4* t = tq + lane * class_pitch4<BM>();
+#pragma unroll
+    for (int j = 0; j < BM / 4; ++j) {
+      t[5 * j + 0] = make_float4(l[4 * j], l[4 * j + 1], l[4 * j + 2], l[4 * j + 3]);
+      t[5 * j + 1] = make_float4(g[4 * j], g[4 * j + 1], g[4 * j + 2], g[4 * j + 3]);
+      t[5 * j + 2] = make_float4(wv[4 * j], wv[4 * j + 1], wv[4 * j + 2], wv[4 * j + 3]);
+      t[5 * j + 3] = make_float4(ph[4 * j], ph[4 * j + 1], ph[4 * j + 2], ph[4 * j + 3]);
+      t[5 * j + 4] = make_float4(ps[4 * j], ps[4 * j + 1], ps[4 * j + 2], ps[4 * j + 3]);
+    }
+  }
+  cp_async_wait_all();
+  __syncwarp();
+  ChunkTabs tabs;
+  tabs.q = tq + lane * class_pitch4<BM>();
+  refine_system<BM, RHS_IDENTITY, SWEEPS, false, PAD, false, BatchWin>(trow, nullptr, tabs, w.nwin, w, lane, range);
+  __syncwarp();
+  {
+    double* gdst = dst + w.off;
+#pragma unroll 4
+    for (int q = 0; q < BM; ++q) {
+      const int r = (int)lane + 32 * q;
+      if (r >= w.out_lo && r < w.out_hi) gdst[r] = trow[tile_off<BM>(r)];
+    }
+  }
+  if (range && status) atomicOr(status, 1u);
+}
+
+constexpr size_t batch_smem() {
+  return (size_t)BW * BTAB * sizeof(float4) + (size_t)BW * sizeof(BatchWin) +
+         (size_t)BW * sys_pitch<BM>() * sizeof(double);
+}
+
+template <int SWEEPS, bool PAD>
+int batch_launch(const double* src, double* dst, const BatchWin* wins, int nwins, unsigned* status,
+                 cudaStream_t st) {
+  if (nwins <= 0) return NTK_OK;
+  auto kern = batch_refine_kernel<SWEEPS, PAD>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_smem());
+  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(batch_refine_kernel)");
+  const unsigned blocks = (unsigned)((nwins + BW - 1) / BW);
+  kern<<<blocks, 32 * BW, batch_smem(), st>>>(src, dst, wins, nwins, status);
+  return cuda_status(cudaGetLastError(), "batch_refine_kernel");
+}
+
+}  // namespace refine_detail
+
+struct BatchRefine {
+  int sweeps = 1;
+  int n_full = 0, n_pad = 0;  // windows of 512 rows, then padded ones
+  BatchWin* d_wins = nullptr;
+  unsigned* d_status = nullptr;
+  ~BatchRefine() {
+    if (d_wins) cudaFree(d_wins);
+    if (d_status) cudaFree(d_status);
+  }
+};
+
+namespace {
+
+DW to_dw(double v) {
+  DW d;
+  d.h = (float)v;
+  d.l = (float)(v - (double)d.h);
+  return d;
+}
+
+}  // namespace
+
+int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const long long* offset,
+                        const double* interior, const double* head, const double* tail, int precision) {
+  using namespace refine_detail;
+  *out = nullptr;
+  // halo for the slowest-decaying system: interior pivot fixed point and
+  // the product of multipliers over H rows below 2^-56
+  std::vector<double> uinf(nsys);
+  double worst = 0.0;
+  for (long long s = 0; s < nsys; ++s) {
+    const double a = interior[3 * s], b = interior[3 * s + 1], c = interior[3 * s + 2];
+    double u = b;
+    for (int i = 0; i < 4096; ++i) {
+      const double un = b - a * c / u;
+      if (un == u || !std::isfinite(un)) break;
+      u = un;
+    }
+    if (!(u != 0.0) || !std::isfinite(u)) {
+      set_error("ntk_batch_create: system %lld has no finite pivot fixed point", s);
+      return NTK_ERR_INVALID;
+    }
+    uinf[s] = u;
+    worst = std::max(worst, std::max(std::fabs(a / u), std::fabs(c / u)));
+  }
+  if (!(worst < 0.75)) {
+    set_error("ntk_batch_create: FP32/refine needs pivots that decay (|a/u|, |c/u| < 0.75; got %g); use NTK_FP64",
+              worst);
+    return NTK_ERR_UNSUPPORTED;
+  }
+  int H = 4;
+  {
+    double prod = 1.0;
+    H = 0;
+    while (prod > std::ldexp(1.0, -56)) {
+      prod *= worst;
+      ++H;
+    }
+    H = (H + 3) & ~1;
+  }
+  const int L = BLW - 2 * H;
+  std::vector<BatchWin> full, padded;
+  for (long long s = 0; s < nsys; ++s) {
+    const int ns = n[s];
+    BatchWin base;
+    base.uinf = (float)uinf[s];
+    base.ai = to_dw(interior[3 * s]);
+    base.bi = to_dw(interior[3 * s + 1]);
+    base.ci = to_dw(interior[3 * s + 2]);
+    base.s = to_dw(1.0);
+    base.unit_scale = 1;
+    // the system's own head rows (0, 1) and tail rows (n-2, n-1); for n = 3
+    // the middle row is head's second row (ntk_batch_create's rule)
+    auto set_head = [&](BatchWin& w) {
+      w.nh = 2;
+      for (int r = 0; r < 2; ++r)
+        for (int k = 0; k < 3; ++k) w.hd[r][k] = to_dw(head[6 * s + 3 * r + k]);
+      w.hd[0][0] = to_dw(0.0);
+    };
+    auto set_tail = [&](BatchWin& w, int nrow) {
+      w.nt = std::min(2, nrow - w.nh);
+      for (int q = 0; q < w.nt; ++q) {
+        const int r = 2 - w.nt + q;  // tail row index within (n-2, n-1)
+        for (int k = 0; k < 3; ++k) w.td[q][k] = to_dw(tail[6 * s + 3 * r + k]);
+      }
+      w.td[w.nt - 1][2] = to_dw(0.0);
+    };
+    auto cut_head = [&](BatchWin& w) {
+      w.nh = 1;
+      w.hd[0][0] = to_dw(0.0);
+      w.hd[0][1] = base.bi;
+      w.hd[0][2] = base.ci;
+    };
+    auto cut_tail = [&](BatchWin& w) {
+      w.nt = 1;
+      w.td[0][0] = base.ai;
+      w.td[0][1] = base.bi;
+      w.td[0][2] = to_dw(0.0);
+    };
+    if (ns <= BLW) {
+      BatchWin w = base;
+      w.off = offset[s];
+      w.nwin = ns;
+      w.out_lo = 0;
+      w.out_hi = ns;
+      set_head(w);
+      if (ns >= 4) {
+        set_tail(w, ns);
+      } else {  // n = 3: rows 0, 1 from head, row 2 from tail's last row
+        w.nt = 1;
+        for (int k = 0; k < 3; ++k) w.td[0][k] = to_dw(tail[6 * s + 3 + k]);
+        w.td[0][2] = to_dw(0.0);
+      }
+      (ns == BLW ? full : padded).push_back(w);
+      continue;
+    }
+    const int Pm1 = (ns - BLW + H + L - 1) / L;
+    const int Pw = Pm1 + 1;
+    for (int g = 0; g < Pw; ++g) {
+      BatchWin w = base;
+      w.nwin = BLW;
+      int start;
+      if (g == 0) {
+        start = 0;
+        w.out_lo = 0;
+        w.out_hi = L;
+        set_head(w);
+        cut_tail(w);
+      } else if (g < Pw - 1) {
+        start = g * L - H;
+        w.out_lo = H;
+        w.out_hi = H + L;
+        cut_head(w);
+        cut_tail(w);
+      } else {
+        start = ns - BLW;
+        w.out_lo = (Pw - 1) * L - start;
+        w.out_hi = BLW;
+        cut_head(w);
+        set_tail(w, BLW);
+      }
+      w.off = offset[s] + start;
+      full.push_back(w);
+    }
+  }
+  BatchRefine* br = new (std::nothrow) BatchRefine();
+  if (!br) {
+    set_error("out of host memory");
+    return NTK_ERR_ALLOC;
+  }
+  br->sweeps = (precision == NTK_FP32) ? 0 : 1;
+  br->n_full = (int)full.size();
+  br->n_pad = (int)padded.size();
+  std::vector<BatchWin> all(full);
+  all.insert(all.end(), padded.begin(), padded.end());
+  int rc = NTK_OK;
+  if (!all.empty()) {
+    rc = cuda_status(cudaMalloc(&br->d_wins, sizeof(BatchWin) * all.size()), "cudaMalloc(batch windows)");
+    if (!rc)
+      rc = cuda_status(cudaMemcpy(br->d_wins, all.data(), sizeof(BatchWin) * all.size(), cudaMemcpyHostToDevice),
+                       "cudaMemcpy(batch windows)");
+  }
+  if (!rc) rc = cuda_status(cudaMalloc(&br->d_status, sizeof(unsigned)), "cudaMalloc(status)");
+  if (!rc) rc = cuda_status(cudaMemset(br->d_status, 0, sizeof(unsigned)), "cudaMemset(status)");
+  if (rc) {
+    delete br;
+    return rc;
+  }
+  *out = br;
+  return NTK_OK;
+}
+
+void batch_refine_destroy(BatchRefine* br) { delete br; }
+
+long long batch_refine_windows(const BatchRefine* br) { return (long long)br->n_full + br->n_pad; }
+
+int batch_refine_solve(BatchRefine* br, double* d, double* work, long long total, cudaStream_t st) {
+  using namespace refine_detail;
+  // windows overlap: read from a copy, write d
+  int rc = cuda_status(cudaMemcpyAsync(work, d, sizeof(double) * (size_t)total, cudaMemcpyDeviceToDevice, st),
+                       "cudaMemcpyAsync(batch input copy)");
+  if (rc) return rc;
+  if (br->sweeps == 0) {
+    rc = batch_launch<0, false>(work, d, br->d_wins, br->n_full, br->d_status, st);
+    if (!rc) rc = batch_launch<0, true>(work, d, br->d_wins + br->n_full, br->n_pad, br->d_status, st);
+  } else {
+    rc = batch_launch<1, false>(work, d, br->d_wins, br->n_full, br->d_status, st);
+    if (!rc) rc = batch_launch<1, true>(work, d, br->d_wins + br->n_full, br->n_pad, br->d_status, st);
+  }
+  return rc;
+}
+
+}  // namespace ntk

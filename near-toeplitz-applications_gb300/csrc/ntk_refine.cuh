@@ -261,7 +261,8 @@ __device__ __forceinline__ long long sys_offset(long long s, const Batch& b) {
 }
 
 // x = s * (h + l) as an FP64 value (no FP64 instruction)
-__device__ __forceinline__ double scaled_out(float h, float l, const RefineArgs& ra) {
+template <class ARGS>
+__device__ __forceinline__ double scaled_out(float h, float l, const ARGS& ra) {
   if (!ra.unit_scale) {
     float p, e, oh, ol;
     two_prod(ra.s.h, h, p, e);
@@ -277,7 +278,8 @@ __device__ __forceinline__ double scaled_out(float h, float l, const RefineArgs&
 // value: s_h * x is split exactly (TwoProd) and the small terms s_h * d and
 // s_l * x are added to its error (s_l * d lies below the double-word's
 // precision), then the pair is normalised and assembled.
-__device__ __forceinline__ double corrected_out(float x, float d, const RefineArgs& ra) {
+template <class ARGS>
+__device__ __forceinline__ double corrected_out(float x, float d, const ARGS& ra) {
   float h, e;
   if (ra.unit_scale) {
     two_sum(x, d, h, e);
@@ -294,9 +296,11 @@ __device__ __forceinline__ double corrected_out(float x, float d, const RefineAr
 // One system, solved by one warp in place in its padded tile trow: RHS
 // (bndw: the double-word right-hand sides of rows 0 and n-1), FP32 solve,
 // refinement sweeps; the FP64 result is left in the tile slots.
-template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY>
+// ARGS: RefineArgs, or any type with the same row-coefficient fields (ai, bi,
+// ci, nh, nt, hd, td) and output scale (s, unit_scale).
+template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY, class ARGS = RefineArgs>
 __device__ __forceinline__ void refine_system(double* trow, const float2* bndw, const ChunkTabs& tabs, int n,
-                                              const RefineArgs& ra, unsigned lane, unsigned& range) {
+                                              const ARGS& ra, unsigned lane, unsigned& range) {
   const int j = lane;
   const int r0 = j * M;
   const int cb = j * (M + 1);  // this lane's chunk in the tile

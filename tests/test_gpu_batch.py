@@ -34,10 +34,10 @@ def _bands(n, interior, head, tail):
     return a, b, c
 
 
-def _check(cuda, oracle, lengths, interior, head, tail, seed, offsets=None):
+def _check(cuda, oracle, lengths, interior, head, tail, seed, offsets=None, precision="fp64"):
     import ntk
 
-    with ntk.UnevenBatch(lengths, interior, head, tail, offsets=offsets) as bt:
+    with ntk.UnevenBatch(lengths, interior, head, tail, offsets=offsets, precision=precision) as bt:
         total = bt.elements
         d = np.random.default_rng(seed).normal(size=total)
         t = torch.from_numpy(d).to(cuda)
@@ -123,3 +123,56 @@ def test_empty_batch(cuda):
 
     with ntk.UnevenBatch(np.zeros(0, int), np.zeros((0, 3)), np.zeros((0, 2, 3)), np.zeros((0, 2, 3))) as bt:
         bt.solve(torch.zeros(1, dtype=torch.float64, device=cuda))
+
+
+# FP32 solve + double-word refinement over overlapping 512-row windows
+# (systems up to 512 rows are one padded window): within 1e-12 relative of
+# the long-double Thomas per system, the refinement tolerance.
+REFINE_TOL = 1e-12
+
+
+def test_refine_uneven_workload_4096(cuda, oracle):
+    from ntk.workloads import uneven_batch
+
+    lengths, systems = uneven_batch(4096, seed=0)
+    interior, head, tail = _descriptors(lengths, systems)
+    worst, _, _, _ = _check(cuda, oracle, lengths, interior, head, tail, seed=1, precision="fp32_refine")
+    assert worst < REFINE_TOL, worst
+
+
+@pytest.mark.parametrize("n", [3, 4, 5, 31, 130, 511, 512, 513, 1000, 20000])
+def test_refine_single_lengths(cuda, oracle, n):
+    rng = np.random.default_rng(n)
+    k = 5
+    lengths = np.full(k, n)
+    interior = np.column_stack([rng.uniform(0.1, 0.3, k), np.ones(k), rng.uniform(0.1, 0.3, k)])
+    head = rng.uniform(-0.3, 0.3, size=(k, 2, 3))
+    head[:, :, 1] = 2.0
+    tail = rng.uniform(-0.3, 0.3, size=(k, 2, 3))
+    tail[:, :, 1] = 2.0
+    worst, _, _, _ = _check(cuda, oracle, lengths, interior, head, tail, seed=n, precision="fp32_refine")
+    assert worst < REFINE_TOL, worst
+
+
+def test_refine_gapped_offsets_leave_gaps_untouched(cuda, oracle):
+    lengths = np.array([50, 700, 90])
+    offsets = np.array([5, 100, 1000])
+    interior = np.tile([0.2, 1.0, 0.25], (3, 1))
+    head = np.tile([[0, 1.5, 0.3], [0.2, 1.2, 0.3]], (3, 1, 1))
+    tail = np.tile([[0.2, 1.1, 0.3], [0.3, 1.4, 0]], (3, 1, 1))
+    worst, _, x, d = _check(cuda, oracle, lengths, interior, head, tail, seed=5, offsets=offsets,
+                            precision="fp32_refine")
+    assert worst < REFINE_TOL
+    untouched = np.ones(len(d), bool)
+    for o, n in zip(offsets, lengths):
+        untouched[o:o + n] = False
+    assert np.array_equal(x[untouched], d[untouched])
+
+
+def test_refine_rejects_slow_decay(cuda):
+    import ntk
+
+    inter = np.array([[0.49, 1.0, 0.49]])
+    hd = np.array([[[0, 1.0, 0.49], [0.49, 1.0, 0.49]]])
+    with pytest.raises(Exception, match="NTK_FP64"):
+        ntk.UnevenBatch([4096], inter, hd, hd, precision="fp32_refine")
