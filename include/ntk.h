@@ -65,9 +65,17 @@ int ntk_plan_create(ntk_plan** out, int n, long long nrhs, const double coeffs[7
  *                           (default), 1 whole-system shared tile, 2 direct
  *   NTK_TUNE_F64_THREADS    threads per block of the one-thread-per-system
  *                           FP64 kernel: 32, 64, 128 (default)
- *   NTK_TUNE_REFINE_W       systems (warps) per CTA of the FP32+refine
- *                           kernel: 4 or 8 (default) */
-enum ntk_tune_key { NTK_TUNE_F64_X_VARIANT = 1, NTK_TUNE_F64_THREADS = 2, NTK_TUNE_REFINE_W = 3 };
+ *   NTK_TUNE_REFINE_W       warps per CTA of the FP32+refine kernel: 4 or
+ *                           8 (default)
+ *   NTK_TUNE_REFINE_SPW     systems per warp of that kernel: 1 (default) or
+ *                           2 (strided layouts with n in 257..512 only; a
+ *                           CTA then stages twice as many adjacent systems) */
+enum ntk_tune_key {
+  NTK_TUNE_F64_X_VARIANT = 1,
+  NTK_TUNE_F64_THREADS = 2,
+  NTK_TUNE_REFINE_W = 3,
+  NTK_TUNE_REFINE_SPW = 4
+};
 int ntk_plan_set_tuning(ntk_plan* plan, int key, int value);
 int ntk_plan_get_tuning(const ntk_plan* plan, int key, int* value);
 

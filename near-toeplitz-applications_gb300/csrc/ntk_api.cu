@@ -227,6 +227,10 @@ int ntk_plan_set_tuning(ntk_plan* plan, int key, int value) {
       if (value != 4 && value != 8) break;
       plan->tune_refine_w = value;
       return NTK_OK;
+    case NTK_TUNE_REFINE_SPW:
+      if (value != 1 && value != 2) break;
+      plan->tune_refine_spw = value;
+      return NTK_OK;
     default:
       ntk::set_error("ntk_plan_set_tuning: unknown key %d", key);
       return NTK_ERR_INVALID;
@@ -244,6 +248,7 @@ int ntk_plan_get_tuning(const ntk_plan* plan, int key, int* value) {
     case NTK_TUNE_F64_X_VARIANT: *value = plan->tune_f64_x_variant; return NTK_OK;
     case NTK_TUNE_F64_THREADS: *value = plan->tune_f64_threads; return NTK_OK;
     case NTK_TUNE_REFINE_W: *value = plan->tune_refine_w; return NTK_OK;
+    case NTK_TUNE_REFINE_SPW: *value = plan->tune_refine_spw; return NTK_OK;
     default:
       ntk::set_error("ntk_plan_get_tuning: unknown key %d", key);
       return NTK_ERR_INVALID;

@@ -72,7 +72,8 @@ struct Plan {
   // launch configuration (ntk_plan_set_tuning; chosen by the autotuner)
   int tune_f64_x_variant = 0;  // contiguous FP64 sweeps: 0 tile ring, 1 whole-system tile, 2 direct
   int tune_f64_threads = 128;  // threads per block of the one-thread-per-system FP64 kernel
-  int tune_refine_w = 8;       // systems (warps) per CTA of the refinement kernel
+  int tune_refine_w = 8;       // warps per CTA of the refinement kernel
+  int tune_refine_spw = 1;     // systems per warp (2: strided layouts, 16 rows per lane)
 
   int init(int n, long long nrhs, const double co[7], int precision, int sweeps);
   ~Plan();

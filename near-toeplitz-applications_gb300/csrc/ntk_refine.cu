@@ -182,15 +182,20 @@ int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsPar
   if (rc) return rc;
   const int W = tune_refine_w;
   const int sweeps_eff = (precision == NTK_FP32) ? 0 : sweeps;
+  // two systems per warp: strided layouts with 16 rows per lane
+  const bool spw2 = (tune_refine_spw == 2) && (M == 16) && (b.es != 1);
   switch (M) {
-    case 4: return refine_dispatch<4, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
-    case 8: return refine_dispatch<8, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+    case 4: return refine_dispatch<4, false, 1>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+    case 8: return refine_dispatch<8, false, 1>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
     case 16:
-      return d ? refine_dispatch<16, true>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream)
-               : refine_dispatch<16, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+      if (spw2)
+        return d ? refine_dispatch<16, true, 2>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream)
+                 : refine_dispatch<16, false, 2>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+      return d ? refine_dispatch<16, true, 1>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream)
+               : refine_dispatch<16, false, 1>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
     default:
-      return d ? refine_dispatch<32, true>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream)
-               : refine_dispatch<32, false>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
+      return d ? refine_dispatch<32, true, 1>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream)
+               : refine_dispatch<32, false, 1>(in, out, n, b, ra, p2, sweeps_eff, rp.kind, W, stream);
   }
 }
 

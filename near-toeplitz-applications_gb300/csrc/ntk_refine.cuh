@@ -68,7 +68,7 @@ struct RefineArgs {
   unsigned* status = nullptr;  // bit 0: input outside the FP32+refine range
 };
 
-template <int M, bool DECAY>
+template <int M, bool DECAY, int SPW>
 int refine_dispatch(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2,
                     int sweeps, int rhs, int W, cudaStream_t st);
 
@@ -233,19 +233,14 @@ struct RefineOcc {
   static constexpr int value = (M <= 16) ? NTK_REFINE_OCC : 1;
 };
 
-// Shared-memory footprint of one CTA: two buffers of W padded system tiles,
-// the class tables (class_pitch4 float4s per class)
-// and, per buffer, the boundary stencils' inputs (3 doubles) and their
-// double-word results for rows 0 and n-1 of each system.
-#ifndef REFINE_GROUPS_PER_CTA
-#define REFINE_GROUPS_PER_CTA 1
-#endif
-constexpr int kRefineBuffers = REFINE_GROUPS_PER_CTA > 1 ? 2 : 1;
+// Shared-memory footprint of one CTA: S padded system tiles, the class
+// tables (class_pitch4 float4s per class), and the boundary stencils'
+// inputs (3 doubles) and double-word results for rows 0 and n-1 of each
+// system.
 template <int M>
-__host__ __device__ constexpr size_t refine_smem(int W, int ncls) {
-  return (((size_t)kRefineBuffers * W * sys_pitch<M>() * sizeof(double) + 15) & ~(size_t)15) +
-         (size_t)ncls * class_pitch4<M>() * sizeof(float4) +
-         (size_t)kRefineBuffers * 2 * W * (sizeof(float2) + 3 * sizeof(double));
+__host__ __device__ constexpr size_t refine_smem(int S, int ncls) {
+  return (((size_t)S * sys_pitch<M>() * sizeof(double) + 15) & ~(size_t)15) +
+         (size_t)ncls * class_pitch4<M>() * sizeof(float4) + (size_t)2 * S * (sizeof(float2) + 3 * sizeof(double));
 }
 
 // Offset of system s's first unknown: (s / ni) * os + (s % ni) * is, with
@@ -505,120 +500,92 @@ __device__ __forceinline__ void refine_system(double* trow, const float2* bndw, 
   }
 }
 
-// ---- staging map of the persistent kernel ----
-// Every thread copies M rows of one system, rows rb + 32q, with rb = lane
-// (contiguous systems: one system per warp, 256-byte rows of copies) or
-// tid / W (strided systems: lanes walk W adjacent systems, blockDim / W ==
-// 32); slot tile_off(rb) + q * QSTEP.  The same thread stores the same rows
-// at the end, so a buffer is reused without a barrier between the stores of
-// one group and the copies of the group after next.
-__device__ __forceinline__ int group_count(const Batch& b, int grp, int W) {
-  const long long left = b.nsys - (long long)grp * W;
-  return (int)(left < W ? left : W);
-}
-__device__ __forceinline__ int map_sw(const Batch& b, int W) {
-  return (b.es == 1) ? (int)(threadIdx.x >> 5) : (int)threadIdx.x % W;
-}
-__device__ __forceinline__ int map_rb(const Batch& b, int W) {
-  return (b.es == 1) ? (int)(threadIdx.x & 31) : (int)threadIdx.x / W;
+// ---- staging map ----
+// A CTA of W warps stages S = SPW * W systems (SPW systems per warp).
+// Contiguous systems (es == 1): warp w copies its systems w + kW, lanes
+// walking rows (256-byte rows of copies).  Strided systems: lanes walk the S
+// adjacent systems (S * 8-byte segments per row), thread t taking system
+// t % S and rows t / S + RS q, RS = 32 W / S rows per step.  Slot of row r:
+// tile_off(r); for a step of RS rows the slot advances by (RS / M)(M + 1).
+// The same thread stores the same rows at the end.
+__device__ __forceinline__ int group_count(const Batch& b, long long grp, int S) {
+  const long long left = b.nsys - grp * S;
+  return (int)(left < S ? left : S);
 }
 
-// issue the copies of group grp into buffer buf (one cp.async group)
-template <int M, int RHS, bool PAD>
-__device__ __forceinline__ void refine_stage(const double* in, double* tiles, double* braw, int n, const Batch& b,
-                                             int grp, int buf, int W) {
+template <int M, int SPW, bool PAD>
+__device__ __forceinline__ void refine_copy(const double* in, double* out, double* tiles, int n, const Batch& b,
+                                            long long grp, int W, bool load) {
   constexpr int P = sys_pitch<M>();
-  constexpr int QSTEP = (32 / M) * (M + 1);
-  const int wc = group_count(b, grp, W);
-  const int sw = map_sw(b, W), rb = map_rb(b, W);
-  if (sw < wc) {
-    const double* gsrc = in + sys_offset((long long)grp * W + sw, b) + (long long)rb * b.es;
-    double* tslot = tiles + (size_t)buf * W * P + sw * P + tile_off<M>(rb);
-    const long long gstep = 32LL * b.es;
-    // the source address is advanced step by step (offsets q * gstep would be
-    // hoisted out of the group loop and held in registers)
+  const int S = SPW * W;
+  const int wc = group_count(b, grp, S);
+  if (b.es == 1) {
+    constexpr int QSTEP = (32 / M) * (M + 1);
+    const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int q = 0; q < M; ++q) {
-      const bool ok = !PAD || rb + 32 * q < n;
-      cp_async8(tslot + q * QSTEP, ok ? gsrc : in, ok ? 8u : 0u);
-      gsrc += gstep;
+    for (int k = 0; k < SPW; ++k) {
+      const int sw = (int)(threadIdx.x >> 5) + k * W;
+      if (sw < wc) {
+        const long long off = sys_offset(grp * S + sw, b) + lane;
+        double* tslot = tiles + (size_t)sw * P + tile_off<M>(lane);
+#pragma unroll
+        for (int q = 0; q < M; ++q) {
+          const bool ok = !PAD || lane + 32 * q < n;
+          if (load)
+            cp_async8(tslot + q * QSTEP, ok ? in + off + 32 * q : in, ok ? 8u : 0u);
+          else if (ok)
+            out[off + 32 * q] = tslot[q * QSTEP];
+        }
+      }
     }
-  }
-  // inputs of the one-sided boundary stencils (compact/rhs.py:21-31): first
-  // warp, lane 2w: rows 0..2 of system w, lane 2w+1: rows n-1..n-3
-  const unsigned lane = threadIdx.x & 31;
-  if (RHS == RHS_COMPACT && threadIdx.x < 32 && (int)(lane >> 1) < wc) {
-    const bool tl = lane & 1;
-    const double* f = in + sys_offset((long long)grp * W + (lane >> 1), b);
-    const long long e = b.es;
-    double* dst = braw + ((size_t)buf * 2 * W + lane) * 3;
-    cp_async8(dst + 0, f + (tl ? (long long)(n - 1) * e : 0), 8u);
-    cp_async8(dst + 1, f + (tl ? (long long)(n - 2) * e : e), 8u);
-    cp_async8(dst + 2, f + (tl ? (long long)(n - 3) * e : 2 * e), 8u);
-  }
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-
-// first warp, once its copies of group grp have landed: the boundary
-// stencils in FP64, one set of FP64 instructions for all W systems
-template <int RHS>
-__device__ __forceinline__ void refine_boundary(const double* braw, float2* bnd, const Batch& b, const RefineArgs& ra,
-                                                int grp, int buf, int W, unsigned& range) {
-  const unsigned lane = threadIdx.x & 31;
-  if (RHS == RHS_COMPACT && (int)(lane >> 1) < group_count(b, grp, W)) {
-    const double* r = braw + ((size_t)buf * 2 * W + lane) * 3;
-    const double v = ((lane & 1) ? ra.sigmaN : ra.sigma0) * ((-5.0 * r[0] + 4.0 * r[1]) + r[2]);
-    float h, l;
-    split_f64(v, h, l, range);
-    fast_two_sum(h, l, h, l);
-    bnd[(size_t)buf * 2 * W + lane] = make_float2(h, l);
-  }
-}
-
-template <int M, bool PAD>
-__device__ __forceinline__ void refine_store(double* out, const double* tiles, int n, const Batch& b, int grp, int buf,
-                                             int W) {
-  constexpr int P = sys_pitch<M>();
-  constexpr int QSTEP = (32 / M) * (M + 1);
-  const int wc = group_count(b, grp, W);
-  const int sw = map_sw(b, W), rb = map_rb(b, W);
-  if (sw < wc) {
-    double* gdst = out + sys_offset((long long)grp * W + sw, b) + (long long)rb * b.es;
-    const double* tslot = tiles + (size_t)buf * W * P + sw * P + tile_off<M>(rb);
-    const long long gstep = 32LL * b.es;
+  } else {
+    constexpr int RS = 32 / SPW;  // rows per step (blockDim / S)
+    static_assert(RS % M == 0, "rows per step must be a multiple of the rows per lane");
+    constexpr int QSTEP = (RS / M) * (M + 1);
+    const int sw = (int)threadIdx.x % S;
+    const int rb = (int)threadIdx.x / S;
+    if (sw < wc) {
+      const long long gstep = (long long)RS * b.es;
+      long long off = sys_offset(grp * S + sw, b) + (long long)rb * b.es;
+      double* tslot = tiles + (size_t)sw * P + tile_off<M>(rb);
+      // the address is advanced step by step (q * gstep offsets would be held
+      // in registers)
 #pragma unroll
-    for (int q = 0; q < M; ++q) {
-      if (!PAD || rb + 32 * q < n) *gdst = tslot[q * QSTEP];
-      gdst += gstep;
+      for (int q = 0; q < M * SPW; ++q) {
+        const bool ok = !PAD || rb + RS * q < n;
+        if (load)
+          cp_async8(tslot + q * QSTEP, ok ? in + off : in, ok ? 8u : 0u);
+        else if (ok)
+          out[off] = tslot[q * QSTEP];
+        off += gstep;
+      }
     }
   }
 }
 
-// Each CTA solves REFINE_GROUPS_PER_CTA consecutive groups of W systems,
-// double-buffered: while the warps solve one group from one tile buffer,
-// the copies of the next group land in the other, so only the first
-// group's load latency is exposed.  Each thread stages and stores the same
-// slots of its buffer, so the only CTA barriers are "group staged" and
-// "group solved".
-template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY>
+// One group of S systems per CTA: stage (cp.async, all copies in flight at
+// once), CTA barrier, each warp solves its SPW systems, CTA barrier, store.
+// The compact scheme's one-sided boundary stencils (compact/rhs.py:21-31)
+// are evaluated in FP64 for all S systems by the first warp (lane 2s: row 0
+// of system s, lane 2s+1: row n-1) from their own small copies: one set of
+// FP64 instructions per CTA instead of one per system.
+template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY, int SPW>
 __global__ void __launch_bounds__(256, RefineOcc<M>::value)
     refine_kernel(const double* in, double* out, int n, Batch b, RefineArgs ra) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int P = sys_pitch<M>();
   const int W = blockDim.x >> 5;
+  const int S = SPW * W;
   const int TC = ra.ncls * class_pitch4<M>();  // table float4s
-  double* tiles = reinterpret_cast<double*>(smem_raw);  // [buffers][W][P]
-  float4* tq = reinterpret_cast<float4*>(smem_raw + (((size_t)kRefineBuffers * W * P * sizeof(double) + 15) &
-                                                     ~(size_t)15));
-  float2* bnd = reinterpret_cast<float2*>(tq + TC);                    // [buffers][2W]: rows 0, n-1
-  double* braw = reinterpret_cast<double*>(bnd + kRefineBuffers * 2 * W);  // [buffers][2W][3]: stencil inputs
+  double* tiles = reinterpret_cast<double*>(smem_raw);  // [S][P]
+  float4* tq = reinterpret_cast<float4*>(smem_raw + (((size_t)S * P * sizeof(double) + 15) & ~(size_t)15));
+  float2* bnd = reinterpret_cast<float2*>(tq + TC);    // [2S]: rows 0, n-1
+  double* braw = reinterpret_cast<double*>(bnd + 2 * S);  // [2S][3]: stencil inputs
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const unsigned lane = tid & 31;
-  // group indices fit in 32 bits (the launcher checks nsys / W < 2^31)
-  const int ngroups = (int)((b.nsys + W - 1) / W);
-  const int g = blockIdx.x * REFINE_GROUPS_PER_CTA;
-  if (g >= ngroups) return;  // whole CTA
+  const long long grp = blockIdx.x;
+  const int wc = group_count(b, grp, S);
   unsigned range = 0;
 
   const int cbase = __ldg(reinterpret_cast<const int*>(ra.tab) + lane) * class_pitch4<M>();
@@ -626,97 +593,91 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
     const float4* g4 = reinterpret_cast<const float4*>(ra.tab + 32);
     for (int i = tid; i < TC; i += blockDim.x) tq[i] = g4[i];
   }
-
-  // The group sequence is unrolled at compile time: a run-time group loop
-  // makes the compiler keep far more values live across its back edge than
-  // the 80 registers of 3 CTAs per SM allow.
-  const int g0 = g;
-#pragma unroll
-  for (int it = 0; it < REFINE_GROUPS_PER_CTA; ++it) {
-    const int buf = it & 1;
-    const int gc = g0 + it;
-    if (it == 0) {
-      refine_stage<M, RHS, PAD>(in, tiles, braw, n, b, gc, 0, W);
-      if (warp == 0) {
-        cp_async_wait_all();
-        __syncwarp();
-        refine_boundary<RHS>(braw, bnd, b, ra, gc, 0, W, range);
-      }
-    }
-    if (gc >= ngroups) break;  // CTA-uniform
-    const int gn = gc + 1;
-    const bool has_next = (it + 1 < REFINE_GROUPS_PER_CTA) && gn < ngroups;  // CTA-uniform
-    if (has_next) {
-      refine_stage<M, RHS, PAD>(in, tiles, braw, n, b, gn, buf ^ 1, W);
-      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-    } else {
-      cp_async_wait_all();
-    }
-    __syncthreads();  // group gc staged (all threads' copies), its bnd written
-    if (warp < group_count(b, gc, W)) {
-      ChunkTabs tabs;
-      tabs.q = tq + cbase;
-      refine_system<M, RHS, SWEEPS, POW2, PAD, DECAY>(tiles + ((size_t)buf * W + warp) * P,
-                                                      bnd + (size_t)buf * 2 * W + 2 * warp, tabs, n, ra, lane, range);
-    }
-    if (warp == 0 && has_next) {
-      cp_async_wait_all();
-      __syncwarp();
-      refine_boundary<RHS>(braw, bnd, b, ra, gn, buf ^ 1, W, range);
-    }
-    __syncthreads();  // group gc solved: results in the tile slots
-    refine_store<M, PAD>(out, tiles, n, b, gc, buf, W);
+  refine_copy<M, SPW, PAD>(in, nullptr, tiles, n, b, grp, W, true);
+  if (RHS == RHS_COMPACT && warp == 0 && (int)(lane >> 1) < wc) {
+    const bool tl = lane & 1;
+    const double* f = in + sys_offset(grp * S + (lane >> 1), b);
+    const long long e = b.es;
+    double* dst = braw + (size_t)lane * 3;
+    cp_async8(dst + 0, f + (tl ? (long long)(n - 1) * e : 0), 8u);
+    cp_async8(dst + 1, f + (tl ? (long long)(n - 2) * e : e), 8u);
+    cp_async8(dst + 2, f + (tl ? (long long)(n - 3) * e : 2 * e), 8u);
   }
+  cp_async_wait_all();
+  if (RHS == RHS_COMPACT && warp == 0) {
+    __syncwarp();
+    if ((int)(lane >> 1) < wc) {
+      const double* r = braw + (size_t)lane * 3;
+      const double v = ((lane & 1) ? ra.sigmaN : ra.sigma0) * ((-5.0 * r[0] + 4.0 * r[1]) + r[2]);
+      float h, l;
+      split_f64(v, h, l, range);
+      fast_two_sum(h, l, h, l);
+      bnd[lane] = make_float2(h, l);
+    }
+  }
+  __syncthreads();  // group staged, boundary right-hand sides written
+  ChunkTabs tabs;
+  tabs.q = tq + cbase;
+#pragma unroll
+  for (int k = 0; k < SPW; ++k) {
+    const int sys = warp + k * W;
+    if (sys < wc)
+      refine_system<M, RHS, SWEEPS, POW2, PAD, DECAY>(tiles + (size_t)sys * P, bnd + 2 * sys, tabs, n, ra, lane,
+                                                      range);
+  }
+  __syncthreads();  // group solved: results in the tile slots
+  refine_copy<M, SPW, PAD>(nullptr, out, tiles, n, b, grp, W, false);
   if (range && ra.status) atomicOr(ra.status, 1u);
 }
 
-template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY>
+template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY, int SPW>
 int launch_one(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, int W, cudaStream_t st) {
-  const size_t smem = refine_smem<M>(W, ra.ncls);
-  auto kern = refine_kernel<M, RHS, SWEEPS, POW2, PAD, DECAY>;
+  const int S = SPW * W;
+  const size_t smem = refine_smem<M>(S, ra.ncls);
+  auto kern = refine_kernel<M, RHS, SWEEPS, POW2, PAD, DECAY, SPW>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(refine_kernel)");
-  const long long groups = (b.nsys + W - 1) / W;
-  if (groups > 0x7fffffffLL) {
+  const long long blocks = (b.nsys + S - 1) / S;
+  if (blocks > 0x7fffffffLL) {
     set_error("too many systems for one launch");
     return NTK_ERR_INVALID;
   }
-  const long long blocks = (groups + REFINE_GROUPS_PER_CTA - 1) / REFINE_GROUPS_PER_CTA;
   kern<<<(unsigned)blocks, W * 32, smem, st>>>(in, out, n, b, ra);
   return cuda_status(cudaGetLastError(), "refine_kernel");
 }
 
-template <int M, int RHS, int SWEEPS, bool DECAY>
+template <int M, int RHS, int SWEEPS, bool DECAY, int SPW>
 int dispatch_pp(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2, int W,
                 cudaStream_t st) {
   const bool pad = (n != 32 * M);
   if (pow2)
-    return pad ? launch_one<M, RHS, SWEEPS, true, true, DECAY>(in, out, n, b, ra, W, st)
-               : launch_one<M, RHS, SWEEPS, true, false, DECAY>(in, out, n, b, ra, W, st);
-  return pad ? launch_one<M, RHS, SWEEPS, false, true, DECAY>(in, out, n, b, ra, W, st)
-             : launch_one<M, RHS, SWEEPS, false, false, DECAY>(in, out, n, b, ra, W, st);
+    return pad ? launch_one<M, RHS, SWEEPS, true, true, DECAY, SPW>(in, out, n, b, ra, W, st)
+               : launch_one<M, RHS, SWEEPS, true, false, DECAY, SPW>(in, out, n, b, ra, W, st);
+  return pad ? launch_one<M, RHS, SWEEPS, false, true, DECAY, SPW>(in, out, n, b, ra, W, st)
+             : launch_one<M, RHS, SWEEPS, false, false, DECAY, SPW>(in, out, n, b, ra, W, st);
 }
 
-template <int M, int RHS, bool DECAY>
+template <int M, int RHS, bool DECAY, int SPW>
 int dispatch_sweeps(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2,
                     int sweeps, int W, cudaStream_t st) {
   switch (sweeps) {
-    case 0: return dispatch_pp<M, RHS, 0, DECAY>(in, out, n, b, ra, pow2, W, st);
-    case 1: return dispatch_pp<M, RHS, 1, DECAY>(in, out, n, b, ra, pow2, W, st);
-    default: return dispatch_pp<M, RHS, 2, DECAY>(in, out, n, b, ra, pow2, W, st);
+    case 0: return dispatch_pp<M, RHS, 0, DECAY, SPW>(in, out, n, b, ra, pow2, W, st);
+    case 1: return dispatch_pp<M, RHS, 1, DECAY, SPW>(in, out, n, b, ra, pow2, W, st);
+    default: return dispatch_pp<M, RHS, 2, DECAY, SPW>(in, out, n, b, ra, pow2, W, st);
   }
 }
 
 }  // namespace refine_detail
 
-// Kernel instances for one M and one carry mode (DECAY); the ntk_refine_m*.cu
-// translation units instantiate them, ntk_refine.cu picks one.
-template <int M, bool DECAY>
+// Kernel instances for one M, one carry mode (DECAY) and one number of
+// systems per warp (SPW); the ntk_refine_m*.cu translation units
+// instantiate them, ntk_refine.cu picks one.
+template <int M, bool DECAY, int SPW>
 int refine_dispatch(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, bool pow2,
                     int sweeps, int rhs, int W, cudaStream_t st) {
   using namespace refine_detail;
-  if (rhs == RHS_COMPACT) return dispatch_sweeps<M, RHS_COMPACT, DECAY>(in, out, n, b, ra, pow2, sweeps, W, st);
-  return dispatch_sweeps<M, RHS_IDENTITY, DECAY>(in, out, n, b, ra, pow2, sweeps, W, st);
+  if (rhs == RHS_COMPACT) return dispatch_sweeps<M, RHS_COMPACT, DECAY, SPW>(in, out, n, b, ra, pow2, sweeps, W, st);
+  return dispatch_sweeps<M, RHS_IDENTITY, DECAY, SPW>(in, out, n, b, ra, pow2, sweeps, W, st);
 }
 
 }  // namespace ntk

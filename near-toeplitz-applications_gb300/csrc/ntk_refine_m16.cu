@@ -2,6 +2,6 @@
 #include "ntk_refine.cuh"
 
 namespace ntk {
-template int refine_dispatch<16, false>(const double*, double*, int, const Batch&, const RefineArgs&, bool, int,
+template int refine_dispatch<16, false, 1>(const double*, double*, int, const Batch&, const RefineArgs&, bool, int,
                                           int, int, cudaStream_t);
 }  // namespace ntk

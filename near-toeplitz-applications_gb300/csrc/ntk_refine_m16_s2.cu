@@ -1,0 +1,7 @@
+// ntk_refine_m16d.cu -- kernel instances of ntk_refine.cuh (one TU per M and carry mode, for parallel builds).
+#include "ntk_refine.cuh"
+
+namespace ntk {
+template int refine_dispatch<16, false, 2>(const double*, double*, int, const Batch&, const RefineArgs&, bool, int,
+                                           int, int, cudaStream_t);
+}  // namespace ntk

@@ -2,8 +2,8 @@
 #include "ntk_refine.cuh"
 
 namespace ntk {
-template int refine_dispatch<4, false>(const double*, double*, int, const Batch&, const RefineArgs&, bool, int,
+template int refine_dispatch<4, false, 1>(const double*, double*, int, const Batch&, const RefineArgs&, bool, int,
                                           int, int, cudaStream_t);
-template int refine_dispatch<8, false>(const double*, double*, int, const Batch&, const RefineArgs&, bool, int,
+template int refine_dispatch<8, false, 1>(const double*, double*, int, const Batch&, const RefineArgs&, bool, int,
                                           int, int, cudaStream_t);
 }  // namespace ntk

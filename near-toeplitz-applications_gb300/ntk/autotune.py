@@ -9,8 +9,10 @@ cached per (device, kernel family, n, precision, layout):
                  shared tile (threads per system = 1 in both)
   f64_threads    threads per block of the one-thread-per-system FP64 kernel
                  (systems per block for the strided sweeps)
-  refine_w       systems (warps) per CTA of the FP32 + refinement kernel
+  refine_w       warps per CTA of the FP32 + refinement kernel
                  (threads per system = 32, rows per lane = n / 32 in registers)
+  refine_spw     systems per warp (2 stages twice as many adjacent systems
+                 per CTA: wider row segments for strided y/z sweeps)
 
 Usage:
     best = autotune.tune(plan, run, key)   # run() launches the workload once
@@ -26,8 +28,8 @@ _lock = threading.Lock()
 
 SPACE = {
     "fp64": {"f64_x_variant": [0, 1], "f64_threads": [64, 128]},
-    "fp32": {"refine_w": [4, 8]},
-    "fp32_refine": {"refine_w": [4, 8]},
+    "fp32": {"refine_w": [4, 8], "refine_spw": [1, 2]},
+    "fp32_refine": {"refine_w": [4, 8], "refine_spw": [1, 2]},
 }
 
 

@@ -18,7 +18,8 @@ def test_candidates_cover_the_space():
 
     c = autotune.candidates("fp64")
     assert {"f64_x_variant": 0, "f64_threads": 64} in c and len(c) == 4
-    assert autotune.candidates("fp32_refine") == [{"refine_w": 4}, {"refine_w": 8}]
+    c = autotune.candidates("fp32_refine")
+    assert len(c) == 4 and {"refine_w": 8, "refine_spw": 2} in c and {"refine_w": 4, "refine_spw": 1} in c
 
 
 def test_tune_picks_fastest_and_caches(tmp_path, monkeypatch):
@@ -27,20 +28,21 @@ def test_tune_picks_fastest_and_caches(tmp_path, monkeypatch):
     monkeypatch.setenv("NTK_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
     monkeypatch.setattr(autotune, "device_name", lambda: "FAKE-GPU")
     plan = FakePlan("fp32_refine")
-    fake_ms = {4: 2.0, 8: 1.0}
+    fake_ms = {(4, 1): 2.0, (8, 1): 1.0, (4, 2): 1.5, (8, 2): 0.5}
+    best = {"refine_w": 8, "refine_spw": 2}
 
     def timer(run, repeats):
-        return fake_ms[plan.cfg["refine_w"]]
+        return fake_ms[(plan.cfg["refine_w"], plan.cfg["refine_spw"])]
 
     res = autotune.tune(plan, lambda: None, key="compact-x", timer=timer)
-    assert res["config"] == {"refine_w": 8} and plan.cfg["refine_w"] == 8
+    assert res["config"] == best and plan.cfg == best
     plan2 = FakePlan("fp32_refine")
-    assert autotune.apply_cached(plan2, "compact-x") == {"refine_w": 8}
-    assert plan2.cfg == {"refine_w": 8}
+    assert autotune.apply_cached(plan2, "compact-x") == best
+    assert plan2.cfg == best
     # a cache hit does not time again
     res2 = autotune.tune(FakePlan("fp32_refine"), lambda: None, key="compact-x",
                          timer=lambda *a: pytest.fail("timed despite cache"))
-    assert res2["config"] == {"refine_w": 8}
+    assert res2["config"] == best
 
 
 @pytest.mark.gpu

@@ -178,3 +178,31 @@ def test_bad_axis_extent_rejected(cuda):
             p.compact_deriv(t, torch.empty_like(t), axis=1, h=0.1)
         with pytest.raises(ValueError):
             p.compact_deriv(t, t[:, :, 1:], axis=2, h=0.1)
+
+
+# Two systems per warp (a CTA stages twice as many adjacent strided
+# systems): same results on strided axes, also with padding (n = 300) and a
+# partial last group; contiguous axes ignore the setting.
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("n,w", [(512, 8), (300, 4), (512, 4)])
+def test_refine_two_systems_per_warp(cuda, oracle, axis, n, w):
+    import ntk
+
+    shape = [9, 7, 9]
+    shape[axis] = n
+    shape = tuple(shape)
+    h = 1.0 / (n - 1)
+    f = fourier_field(shape, seed=n + 3 * axis + w)
+    t = torch.from_numpy(f).to(cuda)
+    ref = oracle.banded_compact_deriv(f, h, axis)
+    out1 = torch.empty_like(t)
+    out2 = torch.empty_like(t)
+    with ntk.Plan(n, 0, COMPACT, precision="fp32_refine") as p:
+        p.set_tuning(refine_w=w, refine_spw=1)
+        p.compact_deriv(t, out1, axis=axis, h=h)
+        p.set_tuning(refine_spw=2)
+        assert p.get_tuning()["refine_spw"] == 2
+        p.compact_deriv(t, out2, axis=axis, h=h)
+        torch.cuda.synchronize()
+    assert oracle.rel_err(out2.cpu().numpy(), ref) < REFINE_TOL
+    assert oracle.rel_err(out2.cpu().numpy(), out1.cpu().numpy()) < REFINE_TOL
