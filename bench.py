@@ -591,23 +591,55 @@ def sample_oracle_errors(f, ref, h, lines=256):
 
 
 def profile_case(which):
-    """Small launches of the hot kernels for `ncu` (no timing): x on a
-    128 x 512 x 512 field, z on 512 x 256 x 256, one warm-up + one launch."""
+    """Small launches of the hot kernels for `ncu` (no timing), each twice
+    (warm-up + measured): compact derivative x on a 128 x 512 x 512 field and
+    z on 512 x 256 x 256 (FP32 + refine with the launch configuration the
+    autotuner picks on GB300 for the benchmark: x W = 4, z W = 8 with two
+    systems per warp; FP64 defaults), `adi` one FP32 + refine ADI step on
+    2048^2 (six window launches), `batch` one FP32 + refine solve of the
+    4096-system uneven batch (two launches)."""
+    import numpy as np
     import torch
 
     import ntk
-    from ntk.workloads import COMPACT_COEFFS, fourier_field
+    from ntk.workloads import COMPACT_COEFFS, fourier_field, gaussians_2d, uneven_batch
 
     dev = torch.device("cuda", 0)
-    fx = fourier_field((128, 512, 512), seed=0, device=dev)
-    fz = fourier_field((512, 256, 256), seed=0, device=dev)
+    tuning = {"refine_x": {"refine_w": 4, "refine_spw": 1}, "refine_z": {"refine_w": 8, "refine_spw": 2}}
+    fields = {}
     for w in which:
+        if w == "adi":
+            NA = 2048
+            dx = 1.0 / (NA - 1)
+            u = gaussians_2d(NA, seed=0, device=dev)
+            x, y = u.clone(), u.t().contiguous()
+            with ntk.Adi(NA, dx, dx * dx, precision="fp32_refine") as adi:
+                for _ in range(2):
+                    adi.step(u, x, y)
+            torch.cuda.synchronize()
+            continue
+        if w == "batch":
+            lengths, systems = uneven_batch(4096, 32, 8192, seed=0)
+            interior = np.array([sy[0] for sy in systems])
+            head = np.array([sy[1] for sy in systems])
+            tail = np.array([sy[2] for sy in systems])
+            with ntk.UnevenBatch(lengths, interior, head, tail, precision="fp32_refine") as bt:
+                t = torch.from_numpy(np.random.default_rng(1).normal(size=bt.elements)).to(dev)
+                for _ in range(2):
+                    bt.solve(t)
+            torch.cuda.synchronize()
+            continue
         prec, ax = w.split("_")
         axis = {"x": 2, "y": 1, "z": 0}[ax]
-        f = fz if ax == "z" else fx
+        shape = (512, 256, 256) if ax == "z" else (128, 512, 512)
+        if shape not in fields:
+            fields[shape] = fourier_field(shape, seed=0, device=dev)
+        f = fields[shape]
         out = torch.empty_like(f)
         n = f.shape[axis]
         with ntk.Plan(n, 0, COMPACT_COEFFS, precision={"refine": "fp32_refine", "fp64": "fp64"}[prec]) as p:
+            if w in tuning:
+                p.set_tuning(**tuning[w])
             for _ in range(2):
                 p.compact_deriv(f, out, axis=axis, h=1.0 / (n - 1))
         torch.cuda.synchronize()

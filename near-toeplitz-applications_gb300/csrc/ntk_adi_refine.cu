@@ -20,8 +20,10 @@
 // residual products) and the right-hand side of the vertical stencil
 // (adi/rhs.py:21-24) becomes  d = gamma * u_mid - (u_lo + u_hi),
 // gamma = 2 (1 - dx^2/dt): one or two FP64 instructions per row, the only
-// FP64 work.  A CTA takes W consecutive systems of one window and stages
-// the W + 2 lines their stencils read with cp.async.
+// FP64 work.  One launch per half step; a CTA takes W consecutive systems
+// of one window, copies its window kind's arguments to shared memory and
+// stages the W + 2 lines their stencils read with cp.async.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -30,73 +32,104 @@
 
 namespace ntk {
 
-struct AdiWin {
-  int out_lo = 0, out_hi = 0;  // window rows written back
-  int head_bnd = 0;            // window row 0 is the system's identity row 0
-  int tail_bnd = 0;            // window row Lw-1 is the system's identity row N-1
-  double gamma = 0.0;          // d = gamma * mid - (lo + hi)
-  const double* bnd = nullptr; // identity-row right-hand sides: system s, system row i at
-  long long bnd_ss = 0;        //   bnd[s * bnd_ss + i * bnd_es]
+// Geometry of one half step: systems s = 0 .. ns-1, system s's row i at
+// in[s * is + i * es]; windows g = 0 .. P-1 of Lw rows (see window_rows).
+struct AdiGeom {
+  long long ns = 0;             // systems (N - 2)
+  long long is = 0, es = 0;     // line and row strides
+  int N = 0, Lw = 0, L = 0, H = 0, P = 1;
+  int whole = 0;                // N == Lw: one window, both identity rows
+  double gamma = 0.0;           // d = gamma * mid - (lo + hi)
+  const double* bnd = nullptr;  // identity-row right-hand sides: system s, row i at
+  long long bnd_ss = 0;         //   bnd[s * bnd_ss + i * bnd_es]
   long long bnd_es = 0;
-  int n_sys = 0;               // system length N
 };
+
+// Window g: first row, rows written back [lo, hi), and its kind (the
+// matrix and tables it uses): 0 first, 1 middle, 2 last, 3 whole.
+struct WinRows {
+  int start, lo, hi, kind;
+};
+__host__ __device__ __forceinline__ WinRows window_rows(const AdiGeom& g, int w) {
+  WinRows r;
+  if (g.whole) {
+    r.start = 0, r.lo = 0, r.hi = g.Lw, r.kind = 3;
+  } else if (w == 0) {
+    r.start = 0, r.lo = 0, r.hi = g.L, r.kind = 0;
+  } else if (w < g.P - 1) {
+    r.start = w * g.L - g.H, r.lo = g.H, r.hi = g.H + g.L, r.kind = 1;
+  } else {
+    r.start = g.N - g.Lw, r.lo = (g.P - 1) * g.L - (g.N - g.Lw), r.hi = g.Lw, r.kind = 2;
+  }
+  return r;
+}
 
 namespace refine_detail {
 
 template <int M>
 __host__ __device__ constexpr size_t adi_smem(int W, int ncls) {
-  // line buffer (W + 2 lines) and W system tiles, padded chunk layout, + tables
-  return (size_t)(2 * W + 2) * sys_pitch<M>() * sizeof(double) + 8 +
+  // line buffer (W + 2 lines) and W system tiles, padded chunk layout, the
+  // window kind's arguments and tables
+  return (size_t)(2 * W + 2) * sys_pitch<M>() * sizeof(double) + 16 + ((sizeof(RefineArgs) + 15) & ~(size_t)15) +
          (size_t)ncls * class_pitch4<M>() * sizeof(float4);
 }
 
-// b: nsys = systems x windows of this launch, ni = systems, is = line
-// stride, os = distance between consecutive windows, es = element stride;
-// in/out point at window row 0 of the launch's first window of system 0.
-// The CTA's W systems are consecutive systems of one window.
+// One launch per half step: CTA b solves window b / nblk of the W
+// consecutive systems starting at (b % nblk) W; args[kind] are the window
+// kinds' kernel arguments (device memory, copied to shared memory).
 template <int M, int SWEEPS, bool POW2, bool DECAY>
 __global__ void __launch_bounds__(256, RefineOcc<M>::value)
-    adi_refine_kernel(const double* in, double* out, Batch b, AdiWin aw, RefineArgs ra) {
+    adi_refine_kernel(const double* in, double* out, AdiGeom geo, const RefineArgs* args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int P = sys_pitch<M>();
   constexpr int LW = 32 * M;
   const int W = blockDim.x >> 5;
-  const int TC = ra.ncls * class_pitch4<M>();
   double* lines = reinterpret_cast<double*>(smem_raw);  // [W + 2][P]
   double* tiles = lines + (size_t)(W + 2) * P;           // [W][P]
-  float4* tq = reinterpret_cast<float4*>(smem_raw + (((size_t)(2 * W + 2) * P * sizeof(double) + 15) & ~(size_t)15));
+  unsigned char* after = smem_raw + (((size_t)(2 * W + 2) * P * sizeof(double) + 15) & ~(size_t)15);
+  RefineArgs* ra = reinterpret_cast<RefineArgs*>(after);
+  float4* tq = reinterpret_cast<float4*>(after + ((sizeof(RefineArgs) + 15) & ~(size_t)15));
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const unsigned lane = tid & 31;
-  const long long nsysw = b.ni;                          // systems per window
-  const long long nblk = (nsysw + W - 1) / W;            // CTAs per window
-  const long long win = blockIdx.x / nblk;
-  const long long s0 = (blockIdx.x % nblk) * W;          // first system of the CTA
-  const int wc = (int)((nsysw - s0) < W ? (nsysw - s0) : W);
+  const long long nblk = (geo.ns + W - 1) / W;  // CTAs per window
+  const int wi = (int)(blockIdx.x / nblk);
+  const long long s0 = (blockIdx.x % nblk) * W;  // first system of the CTA
+  const int wc = (int)((geo.ns - s0) < W ? (geo.ns - s0) : W);
+  const WinRows wr = window_rows(geo, wi);
   unsigned range = 0;
 
-  const int cbase = __ldg(reinterpret_cast<const int*>(ra.tab) + lane) * class_pitch4<M>();
+  // this window kind's arguments and FP32 tables
   {
-    const float4* g4 = reinterpret_cast<const float4*>(ra.tab + 32);
+    const int* src = reinterpret_cast<const int*>(args + wr.kind);
+    int* dst = reinterpret_cast<int*>(ra);
+    constexpr int NW = (int)(sizeof(RefineArgs) / sizeof(int));
+    for (int i = tid; i < NW; i += blockDim.x) dst[i] = __ldg(src + i);
+  }
+  __syncthreads();
+  const int TC = ra->ncls * class_pitch4<M>();
+  const int cbase = __ldg(reinterpret_cast<const int*>(ra->tab) + lane) * class_pitch4<M>();
+  {
+    const float4* g4 = reinterpret_cast<const float4*>(ra->tab + 32);
     for (int i = tid; i < TC; i += blockDim.x) tq[i] = g4[i];
   }
 
   // ---- stage lines s0-1 .. s0+wc (the stencil's neighbours included) ----
   // Line j of the buffer is system line s0 - 1 + j; lanes walk rows for
   // unit element stride (256-byte rows of copies), lines otherwise.
-  const double* wbase = in + win * b.os;
+  const double* wbase = in + (long long)wr.start * geo.es;
   const int nl = wc + 2;
   const int total = nl * LW;
   for (int idx = tid; idx < total; idx += blockDim.x) {
     int j, r;
-    if (b.es == 1) {
+    if (geo.es == 1) {
       j = idx / LW;
       r = idx - j * LW;
     } else {
       r = idx / nl;
       j = idx - r * nl;
     }
-    const double* src = wbase + (s0 - 1 + j) * b.is + (long long)r * b.es;
+    const double* src = wbase + (s0 - 1 + j) * geo.is + (long long)r * geo.es;
     cp_async8(lines + (size_t)j * P + tile_off<M>(r), src, 8u);
   }
   cp_async_wait_all();
@@ -111,71 +144,78 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
     double* trow = tiles + (size_t)warp * P;
     float2* drow = reinterpret_cast<float2*>(trow);
     const long long s = s0 + warp;
+    if (geo.gamma != 0.0) {
 #pragma unroll
-    for (int k = 0; k < M; ++k) {
-      double d = -(lo[cb + k] + hi[cb + k]);
-      if (aw.gamma != 0.0) d = fma(aw.gamma, mid[cb + k], d);
-      float h, l;
-      split_f64(d, h, l, range);
-      drow[cb + k] = make_float2(h, l);
+      for (int k = 0; k < M; ++k) {
+        const double d = fma(geo.gamma, mid[cb + k], (-lo[cb + k]) - hi[cb + k]);
+        float h, l;
+        split_f64(d, h, l, range);
+        drow[cb + k] = make_float2(h, l);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < M; ++k) {
+        float h, l;
+        split_f64((-lo[cb + k]) - hi[cb + k], h, l, range);
+        drow[cb + k] = make_float2(h, l);
+      }
     }
     // identity rows: x = the boundary value (adi/rhs.py leaves them to the
     // solve's first and last rows, experiments/run-adi.py:50-53)
-    if (aw.head_bnd && lane == 0) {
+    if ((wr.kind == 0 || wr.kind == 3) && lane == 0) {
       float h, l;
-      split_f64(aw.bnd[s * aw.bnd_ss], h, l, range);
+      split_f64(geo.bnd[s * geo.bnd_ss], h, l, range);
       drow[0] = make_float2(h, l);
     }
-    if (aw.tail_bnd && lane == 31) {
+    if ((wr.kind == 2 || wr.kind == 3) && lane == 31) {
       float h, l;
-      split_f64(aw.bnd[s * aw.bnd_ss + (long long)(aw.n_sys - 1) * aw.bnd_es], h, l, range);
+      split_f64(geo.bnd[s * geo.bnd_ss + (long long)(geo.N - 1) * geo.bnd_es], h, l, range);
       drow[tile_off<M>(LW - 1)] = make_float2(h, l);
     }
     __syncwarp();
     ChunkTabs tabs;
     tabs.q = tq + cbase;
-    refine_system<M, RHS_PRESPLIT, SWEEPS, POW2, false, DECAY>(trow, nullptr, tabs, LW, ra, lane, range);
+    refine_system<M, RHS_PRESPLIT, SWEEPS, POW2, false, DECAY>(trow, nullptr, tabs, LW, *ra, lane, range);
     __syncwarp();
     // ---- write back the window's central rows (coalesced for unit stride) ----
-    double* dst = out + win * b.os + s * b.is;
+    double* dst = out + (long long)wr.start * geo.es + s * geo.is;
 #pragma unroll 4
     for (int q = 0; q < M; ++q) {
       const int r = (int)lane + 32 * q;
-      if (r >= aw.out_lo && r < aw.out_hi) dst[(long long)r * b.es] = trow[tile_off<M>(r)];
+      if (r >= wr.lo && r < wr.hi) dst[(long long)r * geo.es] = trow[tile_off<M>(r)];
     }
   }
-  if (range && ra.status) atomicOr(ra.status, 1u);
+  if (range && ra->status) atomicOr(ra->status, 1u);
 }
 
 template <int M, int SWEEPS, bool POW2, bool DECAY>
-int adi_launch(const double* in, double* out, const Batch& b, const AdiWin& aw, const RefineArgs& ra, int W,
+int adi_launch(const double* in, double* out, const AdiGeom& geo, const RefineArgs* d_args, int max_ncls, int W,
                cudaStream_t st) {
-  const size_t smem = adi_smem<M>(W, ra.ncls);
+  const size_t smem = adi_smem<M>(W, max_ncls);
   auto kern = adi_refine_kernel<M, SWEEPS, POW2, DECAY>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(adi_refine_kernel)");
-  const long long windows = b.nsys / b.ni;
-  const long long blocks = windows * ((b.ni + W - 1) / W);
+  const long long blocks = (long long)geo.P * ((geo.ns + W - 1) / W);
   if (blocks <= 0) return NTK_OK;
   if (blocks > 0x7fffffffLL) {
     set_error("too many ADI windows for one launch");
     return NTK_ERR_INVALID;
   }
-  kern<<<(unsigned)blocks, W * 32, smem, st>>>(in, out, b, aw, ra);
+  kern<<<(unsigned)blocks, W * 32, smem, st>>>(in, out, geo, d_args);
   return cuda_status(cudaGetLastError(), "adi_refine_kernel");
 }
 
 template <int M, bool DECAY>
-int adi_dispatch(const double* in, double* out, const Batch& b, const AdiWin& aw, const RefineArgs& ra, bool pow2,
-                 int sweeps, int W, cudaStream_t st) {
+int adi_dispatch(const double* in, double* out, const AdiGeom& geo, const RefineArgs* d_args, int max_ncls,
+                 bool pow2, int sweeps, int W, cudaStream_t st) {
   if (sweeps == 0)
-    return pow2 ? adi_launch<M, 0, true, DECAY>(in, out, b, aw, ra, W, st)
-                : adi_launch<M, 0, false, DECAY>(in, out, b, aw, ra, W, st);
+    return pow2 ? adi_launch<M, 0, true, DECAY>(in, out, geo, d_args, max_ncls, W, st)
+                : adi_launch<M, 0, false, DECAY>(in, out, geo, d_args, max_ncls, W, st);
   if (sweeps == 1)
-    return pow2 ? adi_launch<M, 1, true, DECAY>(in, out, b, aw, ra, W, st)
-                : adi_launch<M, 1, false, DECAY>(in, out, b, aw, ra, W, st);
-  return pow2 ? adi_launch<M, 2, true, DECAY>(in, out, b, aw, ra, W, st)
-              : adi_launch<M, 2, false, DECAY>(in, out, b, aw, ra, W, st);
+    return pow2 ? adi_launch<M, 1, true, DECAY>(in, out, geo, d_args, max_ncls, W, st)
+                : adi_launch<M, 1, false, DECAY>(in, out, geo, d_args, max_ncls, W, st);
+  return pow2 ? adi_launch<M, 2, true, DECAY>(in, out, geo, d_args, max_ncls, W, st)
+              : adi_launch<M, 2, false, DECAY>(in, out, geo, d_args, max_ncls, W, st);
 }
 
 }  // namespace refine_detail
@@ -187,6 +227,12 @@ struct AdiRefine {
   double gamma = 0.0;
   bool whole = false;  // N == Lw: one window per system, no truncation
   Plan win[4];         // first, middle, last, whole window matrices (n = Lw)
+  RefineArgs* d_args = nullptr;  // kernel arguments of the four kinds (device)
+  int max_ncls = 1;
+  bool pow2 = true, decay = true;
+  ~AdiRefine() {
+    if (d_args) cudaFree(d_args);
+  }
 };
 
 int adi_refine_create(AdiRefine** out, int N, double dx, double dt, int precision) {
@@ -261,6 +307,31 @@ int adi_refine_create(AdiRefine** out, int N, double dx, double dt, int precisio
       return rc;
     }
   }
+  // the kinds' kernel arguments, uploaded once; one kernel shape for all
+  // (power-of-two rows and one-shuffle carries only if every kind has them)
+  {
+    RefineArgs host[4];
+    for (int k = 0; k < 4; ++k) {
+      if ((k == 3) != ar->whole) continue;
+      int M = 0;
+      bool p2 = false, dec = false;
+      int rc = refine_args(ar->win[k], 1.0, 1.0, 1.0, &host[k], &M, &p2, &dec);
+      if (rc) {
+        delete ar;
+        return rc;
+      }
+      ar->pow2 = ar->pow2 && p2;
+      ar->decay = ar->decay && dec;
+      ar->max_ncls = std::max(ar->max_ncls, host[k].ncls);
+    }
+    int rc = cuda_status(cudaMalloc(&ar->d_args, sizeof(host)), "cudaMalloc(ADI window arguments)");
+    if (!rc) rc = cuda_status(cudaMemcpy(ar->d_args, host, sizeof(host), cudaMemcpyHostToDevice),
+                              "cudaMemcpy(ADI window arguments)");
+    if (rc) {
+      delete ar;
+      return rc;
+    }
+  }
   *out = ar;
   return NTK_OK;
 }
@@ -275,76 +346,32 @@ void adi_refine_windows(const AdiRefine* ar, int* L, int* H, int* P) {
 
 namespace {
 
-int run_windows(AdiRefine* ar, int kind, const double* in, double* out, Batch b, AdiWin aw, int W, cudaStream_t st) {
-  RefineArgs ra;
-  int M = 0;
-  bool p2 = false, dec = false;
-  int rc = refine_args(ar->win[kind], 1.0, 1.0, 1.0, &ra, &M, &p2, &dec);
-  if (rc) return rc;
-  using namespace refine_detail;
-  switch (M) {
-    case 4: return adi_dispatch<4, false>(in, out, b, aw, ra, p2, ar->sweeps, W, st);
-    case 8: return adi_dispatch<8, false>(in, out, b, aw, ra, p2, ar->sweeps, W, st);
-    default:
-      return dec ? adi_dispatch<16, true>(in, out, b, aw, ra, p2, ar->sweeps, W, st)
-                 : adi_dispatch<16, false>(in, out, b, aw, ra, p2, ar->sweeps, W, st);
-  }
-}
-
 // One half step: systems s = 0..N-3 are lines s+1 of the field; in/out point
 // at system 0's row 0; `is` is the line stride, `es` the row stride.
 int half_step(AdiRefine* ar, const double* in, double* out, long long is, long long es, const double* bnd,
               long long bnd_ss, long long bnd_es, int W, cudaStream_t st) {
-  const int N = ar->N, Lw = ar->Lw, H = ar->H, L = ar->L, P = ar->P;
-  AdiWin aw;
-  aw.gamma = ar->gamma;
-  aw.bnd = bnd;
-  aw.bnd_ss = bnd_ss;
-  aw.bnd_es = bnd_es;
-  aw.n_sys = N;
-  Batch b;
-  b.ni = N - 2;
-  b.is = is;
-  b.es = es;
-  if (ar->whole) {
-    b.nsys = b.ni;
-    b.os = 0;
-    aw.out_lo = 0;
-    aw.out_hi = Lw;
-    aw.head_bnd = 1;
-    aw.tail_bnd = 1;
-    return run_windows(ar, 3, in, out, b, aw, W, st);
+  AdiGeom g;
+  g.ns = ar->N - 2;
+  g.is = is;
+  g.es = es;
+  g.N = ar->N;
+  g.Lw = ar->Lw;
+  g.L = ar->L;
+  g.H = ar->H;
+  g.P = ar->P;
+  g.whole = ar->whole ? 1 : 0;
+  g.gamma = ar->gamma;
+  g.bnd = bnd;
+  g.bnd_ss = bnd_ss;
+  g.bnd_es = bnd_es;
+  using namespace refine_detail;
+  switch (ar->M) {
+    case 4: return adi_dispatch<4, false>(in, out, g, ar->d_args, ar->max_ncls, ar->pow2, ar->sweeps, W, st);
+    case 8: return adi_dispatch<8, false>(in, out, g, ar->d_args, ar->max_ncls, ar->pow2, ar->sweeps, W, st);
+    default:
+      return ar->decay ? adi_dispatch<16, true>(in, out, g, ar->d_args, ar->max_ncls, ar->pow2, ar->sweeps, W, st)
+                       : adi_dispatch<16, false>(in, out, g, ar->d_args, ar->max_ncls, ar->pow2, ar->sweeps, W, st);
   }
-  // first windows
-  b.nsys = b.ni;
-  b.os = 0;
-  aw.out_lo = 0;
-  aw.out_hi = L;
-  aw.head_bnd = 1;
-  aw.tail_bnd = 0;
-  int rc = run_windows(ar, 0, in, out, b, aw, W, st);
-  if (rc) return rc;
-  // middle windows g = 1 .. P-2 (window start gL - H)
-  if (P > 2) {
-    b.nsys = b.ni * (P - 2);
-    b.os = (long long)L * es;
-    aw.out_lo = H;
-    aw.out_hi = H + L;
-    aw.head_bnd = 0;
-    aw.tail_bnd = 0;
-    const long long off = (long long)(L - H) * es;
-    rc = run_windows(ar, 1, in + off, out + off, b, aw, W, st);
-    if (rc) return rc;
-  }
-  // last windows: [N - Lw, N), writing rows (P-1) L .. N-1
-  b.nsys = b.ni;
-  b.os = 0;
-  aw.out_lo = (P - 1) * L - (N - Lw);
-  aw.out_hi = Lw;
-  aw.head_bnd = 0;
-  aw.tail_bnd = 1;
-  const long long off = (long long)(N - Lw) * es;
-  return run_windows(ar, 2, in + off, out + off, b, aw, W, st);
 }
 
 }  // namespace
