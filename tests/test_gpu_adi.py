@@ -134,7 +134,7 @@ def _run(cuda, u0, dx, dt, steps, precision, graph):
 
 # FP32 solve + double-word refinement per half step, over overlapping
 # windows (or one whole-system window when N equals the window length):
-# within 1e-12 of the FP64 path (the benchmark spec's refinement tolerance), also
+# within 1e-12 of the FP64 path (the refinement tolerance), also
 # for a non-power-of-two N, middle windows (N = 1000, 2048) and a slowly
 # decaying, badly conditioned matrix (r = 40, two sweeps).
 @pytest.mark.parametrize("N,r,steps", [(128, 0.5, 5), (256, 0.5, 10), (300, 0.5, 5), (512, 0.5, 5),
