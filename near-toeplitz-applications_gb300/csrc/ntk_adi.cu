@@ -37,7 +37,6 @@ struct Adi {
   SegParams sp;
   double bottom = 0, center = 0, top = 0;
   AdiRefine* refine = nullptr;  // NTK_FP32 / NTK_FP32_REFINE half steps (ntk_adi_refine.cu)
-  int refine_w = 4;             // systems per CTA of the refinement windows
   cudaStream_t capture_stream = nullptr;
   std::map<std::tuple<const void*, const void*, const void*, int>, cudaGraphExec_t> graphs;
 
@@ -56,7 +55,7 @@ namespace {
 }  // namespace
 
 int adi_step(Adi* a, double* u, double* d_x, const double* d_y, cudaStream_t st) {
-  if (a->refine) return adi_refine_step(a->refine, u, d_x, d_y, a->refine_w, st);
+  if (a->refine) return adi_refine_step(a->refine, u, d_x, d_y, st);
   const int N = a->N;
   TablesF64 t;
   t.l = a->plan.d_lw;

@@ -64,13 +64,21 @@ __host__ __device__ __forceinline__ WinRows window_rows(const AdiGeom& g, int w)
   return r;
 }
 
+#ifndef NTK_ADI_WX
+#define NTK_ADI_WX 4
+#endif
+#ifndef NTK_ADI_WY
+#define NTK_ADI_WY 8
+#endif
+
 namespace refine_detail {
 
 template <int M>
 __host__ __device__ constexpr size_t adi_smem(int W, int ncls) {
-  // line buffer (W + 2 lines) and W system tiles, padded chunk layout, the
-  // window kind's arguments and tables
-  return (size_t)(2 * W + 2) * sys_pitch<M>() * sizeof(double) + 16 + ((sizeof(RefineArgs) + 15) & ~(size_t)15) +
+  // line buffer (W + 2 lines, padded chunk layout; system w's tile reuses
+  // line w + 1 once the stencil is formed), the window kind's arguments and
+  // tables
+  return (size_t)(W + 2) * sys_pitch<M>() * sizeof(double) + 16 + ((sizeof(RefineArgs) + 15) & ~(size_t)15) +
          (size_t)ncls * class_pitch4<M>() * sizeof(float4);
 }
 
@@ -85,8 +93,7 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
   constexpr int LW = 32 * M;
   const int W = blockDim.x >> 5;
   double* lines = reinterpret_cast<double*>(smem_raw);  // [W + 2][P]
-  double* tiles = lines + (size_t)(W + 2) * P;           // [W][P]
-  unsigned char* after = smem_raw + (((size_t)(2 * W + 2) * P * sizeof(double) + 15) & ~(size_t)15);
+  unsigned char* after = smem_raw + (((size_t)(W + 2) * P * sizeof(double) + 15) & ~(size_t)15);
   RefineArgs* ra = reinterpret_cast<RefineArgs*>(after);
   float4* tq = reinterpret_cast<float4*>(after + ((sizeof(RefineArgs) + 15) & ~(size_t)15));
   const int tid = threadIdx.x;
@@ -135,43 +142,35 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
   cp_async_wait_all();
   __syncthreads();
 
+  // ---- double-word right-hand side, first in registers: every warp reads
+  // three lines, and system w's tile then reuses line w + 1 ----
+  const int cb = (int)lane * (M + 1);
+  const long long s = s0 + warp;
+  float dh[M], dl[M];
   if (warp < wc) {
-    // ---- double-word right-hand side into this system's tile ----
-    const int cb = (int)lane * (M + 1);
     const double* lo = lines + (size_t)warp * P;
     const double* mid = lo + P;
     const double* hi = mid + P;
-    double* trow = tiles + (size_t)warp * P;
-    float2* drow = reinterpret_cast<float2*>(trow);
-    const long long s = s0 + warp;
     if (geo.gamma != 0.0) {
 #pragma unroll
-      for (int k = 0; k < M; ++k) {
-        const double d = fma(geo.gamma, mid[cb + k], (-lo[cb + k]) - hi[cb + k]);
-        float h, l;
-        split_f64(d, h, l, range);
-        drow[cb + k] = make_float2(h, l);
-      }
+      for (int k = 0; k < M; ++k)
+        split_f64(fma(geo.gamma, mid[cb + k], (-lo[cb + k]) - hi[cb + k]), dh[k], dl[k], range);
     } else {
 #pragma unroll
-      for (int k = 0; k < M; ++k) {
-        float h, l;
-        split_f64((-lo[cb + k]) - hi[cb + k], h, l, range);
-        drow[cb + k] = make_float2(h, l);
-      }
+      for (int k = 0; k < M; ++k) split_f64((-lo[cb + k]) - hi[cb + k], dh[k], dl[k], range);
     }
     // identity rows: x = the boundary value (adi/rhs.py leaves them to the
     // solve's first and last rows, experiments/run-adi.py:50-53)
-    if ((wr.kind == 0 || wr.kind == 3) && lane == 0) {
-      float h, l;
-      split_f64(geo.bnd[s * geo.bnd_ss], h, l, range);
-      drow[0] = make_float2(h, l);
-    }
-    if ((wr.kind == 2 || wr.kind == 3) && lane == 31) {
-      float h, l;
-      split_f64(geo.bnd[s * geo.bnd_ss + (long long)(geo.N - 1) * geo.bnd_es], h, l, range);
-      drow[tile_off<M>(LW - 1)] = make_float2(h, l);
-    }
+    if ((wr.kind == 0 || wr.kind == 3) && lane == 0) split_f64(geo.bnd[s * geo.bnd_ss], dh[0], dl[0], range);
+    if ((wr.kind == 2 || wr.kind == 3) && lane == 31)
+      split_f64(geo.bnd[s * geo.bnd_ss + (long long)(geo.N - 1) * geo.bnd_es], dh[M - 1], dl[M - 1], range);
+  }
+  __syncthreads();  // all lines read
+  if (warp < wc) {
+    double* trow = lines + (size_t)(warp + 1) * P;
+    float2* drow = reinterpret_cast<float2*>(trow);
+#pragma unroll
+    for (int k = 0; k < M; ++k) drow[cb + k] = make_float2(dh[k], dl[k]);
     __syncwarp();
     ChunkTabs tabs;
     tabs.q = tq + cbase;
@@ -227,6 +226,9 @@ struct AdiRefine {
   double gamma = 0.0;
   bool whole = false;  // N == Lw: one window per system, no truncation
   Plan win[4];         // first, middle, last, whole window matrices (n = Lw)
+  // systems per CTA: rows (x half step) are staged as 256-byte row segments
+  // already; columns (y half step) gain from more adjacent columns per CTA
+  int wx = NTK_ADI_WX, wy = NTK_ADI_WY;
   RefineArgs* d_args = nullptr;  // kernel arguments of the four kinds (device)
   int max_ncls = 1;
   bool pow2 = true, decay = true;
@@ -376,13 +378,13 @@ int half_step(AdiRefine* ar, const double* in, double* out, long long is, long l
 
 }  // namespace
 
-int adi_refine_step(AdiRefine* ar, double* u, double* d_x, const double* d_y, int W, cudaStream_t st) {
+int adi_refine_step(AdiRefine* ar, double* u, double* d_x, const double* d_y, cudaStream_t st) {
   const int N = ar->N;
   // x half: systems = rows 1..N-2, stencil of u's rows, boundary RHS from d_x
-  int rc = half_step(ar, u + N, d_x + N, N, 1, d_x + N, N, 1, W, st);
+  int rc = half_step(ar, u + N, d_x + N, N, 1, d_x + N, N, 1, ar->wx, st);
   if (rc) return rc;
   // y half: systems = columns 1..N-2 of d_x, result into u, boundary RHS from d_y
-  return half_step(ar, d_x + 1, u + 1, 1, N, d_y + N, N, 1, W, st);
+  return half_step(ar, d_x + 1, u + 1, 1, N, d_y + N, N, 1, ar->wy, st);
 }
 
 }  // namespace ntk

@@ -15,7 +15,7 @@ void adi_refine_destroy(AdiRefine* ar);
 // rows each window writes back, halo (0 for one whole-system window) and
 // windows per system
 void adi_refine_windows(const AdiRefine* ar, int* L, int* H, int* P);
-// one step (both half steps) in place, W systems per CTA
-int adi_refine_step(AdiRefine* ar, double* u, double* d_x, const double* d_y, int W, cudaStream_t st);
+// one step (both half steps) in place
+int adi_refine_step(AdiRefine* ar, double* u, double* d_x, const double* d_y, cudaStream_t st);
 
 }  // namespace ntk
