@@ -45,7 +45,12 @@ namespace refine_detail {
 constexpr int BM = 16;                  // rows per lane
 constexpr int BLW = 32 * BM;            // window rows
 constexpr int BW = 4;                   // warps (windows) per CTA
-constexpr int BTAB = 32 * class_pitch4<BM>();  // float4s of one warp's tables
+// Table slots of one warp: lanes whose chunks (and the three rows before
+// them) see the same coefficients build identical tables, so they share a
+// slot: 0 lane 0 (the window's head), 1 interior lanes, 2..4 the lanes
+// around the system's tail rows, 5 lanes wholly in the padding.
+constexpr int BSLOTS = 6;
+constexpr int BTAB = BSLOTS * class_pitch4<BM>();  // float4s of one warp's tables
 
 __device__ __forceinline__ void row_coeffs(const BatchWin& w, int r, float& a, float& b, float& c) {
   if (r >= w.nwin) {
@@ -68,8 +73,38 @@ __device__ __forceinline__ void row_coeffs(const BatchWin& w, int r, float& a, f
   }
 }
 
+// Slot of lane j (its table depends on rows 16j - 3 .. 16j + 15): lane 0
+// alone; lanes whose rows reach the tail rows or the padding start
+// (16j + 15 >= nwin - nt and 16j - 3 < nwin) by position; lanes wholly in
+// the padding (16j - 3 >= nwin) one slot; all other lanes one interior slot.
+// The writer of a slot is the first lane that maps to it.
+__device__ __forceinline__ void slot_of(const BatchWin& w, int j, int& slot, bool& writer) {
+  const int r0 = j * BM;
+  if (j == 0) {
+    slot = 0;
+    writer = true;
+    return;
+  }
+  // first lane reaching the tail region
+  const int jft = max(1, (w.nwin - w.nt - (BM - 1) + (BM - 1)) / BM);
+  if (r0 - 3 >= w.nwin) {
+    // wholly padding: the first such lane writes
+    const int jpad = max(1, (w.nwin + 3 + BM - 1) / BM);
+    slot = 5;
+    writer = (j == jpad);
+    return;
+  }
+  if (j >= jft) {
+    slot = 2 + min(j - jft, 2);
+    writer = (j - jft) <= 2;
+    return;
+  }
+  slot = 1;
+  writer = (j == 1);
+}
+
 template <int SWEEPS, bool PAD>
-__global__ void __launch_bounds__(32 * BW) batch_refine_kernel(const double* __restrict__ src, double* dst,
+__global__ void __launch_bounds__(32 * BW, 6) batch_refine_kernel(const double* __restrict__ src, double* dst,
                                                                const BatchWin* __restrict__ wins, int nwins,
                                                                unsigned* status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -147,7 +182,12 @@ __global__ void __launch_bounds__(32 * BW) batch_refine_kernel(const double* __r
       psi *= -wv[k];
       ps[k] = psi;
     }
-    float4* t = tq + lane * class_pitch4<BM>();
+    // this lane's slot, and whether it writes it (one writer per slot)
+    int slot;
+    bool writer;
+    slot_of(w, (int)lane, slot, writer);
+    float4* t = tq + slot * class_pitch4<BM>();
+    if (writer)
 #pragma unroll
     for (int j = 0; j < BM / 4; ++j) {
       t[5 * j + 0] = make_float4(l[4 * j], l[4 * j + 1], l[4 * j + 2], l[4 * j + 3]);
@@ -160,7 +200,12 @@ __global__ void __launch_bounds__(32 * BW) batch_refine_kernel(const double* __r
   cp_async_wait_all();
   __syncwarp();
   ChunkTabs tabs;
-  tabs.q = tq + lane * class_pitch4<BM>();
+  {
+    int slot;
+    bool writer;
+    slot_of(w, (int)lane, slot, writer);
+    tabs.q = tq + slot * class_pitch4<BM>();
+  }
   refine_system<BM, RHS_IDENTITY, SWEEPS, false, PAD, false, BatchWin>(trow, nullptr, tabs, w.nwin, w, lane, range);
   __syncwarp();
   {
