@@ -54,7 +54,12 @@ int ntk_last_error(char* buf, int len);
  * (neato.py:199-274) become the shared matrix's LU factors, computed once in
  * FP64 on the host and uploaded.  nrhs is the number of contiguous systems
  * ntk_solve works on (neato.py:135-136).  precision is an ntk_precision;
- * refine_sweeps (>= 1) is used by NTK_FP32_REFINE.  Synchronous. */
+ * refine_sweeps (>= 1) is used by NTK_FP32_REFINE.  FP32 paths: n <= 1024
+ * runs one warp per system; longer systems run as overlapping 512-row
+ * windows (NTK_ERR_UNSUPPORTED when the LU multipliers |a/u|, |c/u| of the
+ * interior are >= 0.9, too slow a decay for the windows), and an in-place
+ * call on them copies its input to a work array the plan allocates on first
+ * use.  Synchronous. */
 int ntk_plan_create(ntk_plan** out, int n, long long nrhs, const double coeffs[7], int precision,
                     int refine_sweeps);
 

@@ -55,6 +55,7 @@ struct Matrix {
 bool factor_host(const Matrix& m, std::vector<double>& l, std::vector<double>& u);
 
 struct RefineState;  // ntk_refine.cu
+struct LongRefine;   // ntk_long_refine.cu
 
 struct Plan {
   int n = 0;
@@ -68,6 +69,7 @@ struct Plan {
   double* d_lw = nullptr;           // device: l[n], w[n]
   std::map<double, double*> g_by_scale;  // device g = s/u per RHS scale
   RefineState* refine = nullptr;
+  LongRefine* long_refine = nullptr;  // FP32 / FP32+refine windows for n > 1024
   std::mutex mu;
   // launch configuration (ntk_plan_set_tuning; chosen by the autotuner)
   int tune_f64_x_variant = 0;  // contiguous FP64 sweeps: 0 tile ring, 1 whole-system tile, 2 direct

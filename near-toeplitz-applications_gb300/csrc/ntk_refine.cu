@@ -5,6 +5,7 @@
 #include <cstring>
 #include <vector>
 
+#include "ntk_long_refine.h"
 #include "ntk_refine.cuh"
 
 namespace ntk {
@@ -53,8 +54,9 @@ int Plan::init_refine() {
       break;
     }
   if (M == 0) {
-    set_error("FP32/refine precision supports n <= 1024 in this build (got %d); use NTK_FP64", n);
-    return NTK_ERR_UNSUPPORTED;
+    // longer than one warp's register tile: overlapping windows
+    // (ntk_long_refine.cu); the plan keeps no per-row tables of its own
+    return long_refine_create(&long_refine, *this, precision, sweeps);
   }
   st->M = M;
   st->n_pad = 32 * M;
@@ -154,6 +156,10 @@ int Plan::init_refine() {
 }
 
 void Plan::release_refine() {
+  if (long_refine) {
+    long_refine_destroy(long_refine);
+    long_refine = nullptr;
+  }
   if (!refine) return;
   if (refine->d_tab) cudaFree(refine->d_tab);
   if (refine->d_status) cudaFree(refine->d_status);
@@ -163,6 +169,13 @@ void Plan::release_refine() {
 
 int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsParams& rp, double s,
                      cudaStream_t stream) {
+  if (long_refine) {
+    if (rp.kind != RHS_IDENTITY && rp.kind != RHS_COMPACT) {
+      set_error("FP32/refine supports the identity and compact right-hand sides");
+      return NTK_ERR_UNSUPPORTED;
+    }
+    return long_refine_run(long_refine, in, out, b, rp, s, tune_refine_w, stream);
+  }
   if (!refine || !refine->d_tab) {
     set_error("plan has no FP32 tables");
     return NTK_ERR_INVALID;

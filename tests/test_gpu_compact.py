@@ -206,3 +206,26 @@ def test_refine_two_systems_per_warp(cuda, oracle, axis, n, w):
         torch.cuda.synchronize()
     assert oracle.rel_err(out2.cpu().numpy(), ref) < REFINE_TOL
     assert oracle.rel_err(out2.cpu().numpy(), out1.cpu().numpy()) < REFINE_TOL
+
+
+# Compact derivatives along systems longer than 1024 rows (windows), each
+# axis, out of place and in place.
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("n", [2048, 1300])
+def test_refine_long_derivative(cuda, oracle, axis, n):
+    import ntk
+
+    shape = [3, 5, 4]
+    shape[axis] = n
+    shape = tuple(shape)
+    h = 1.0 / (n - 1)
+    f = fourier_field(shape, seed=n + axis)
+    ref = oracle.banded_compact_deriv(f, h, axis)
+    t = torch.from_numpy(f).to(cuda)
+    out = torch.empty_like(t)
+    with ntk.Plan(n, 0, COMPACT, precision="fp32_refine") as p:
+        p.compact_deriv(t, out, axis=axis, h=h)
+        p.compact_deriv(t, t, axis=axis, h=h)  # in place
+        torch.cuda.synchronize()
+    assert oracle.rel_err(out.cpu().numpy(), ref) < REFINE_TOL
+    assert oracle.rel_err(t.cpu().numpy(), ref) < REFINE_TOL

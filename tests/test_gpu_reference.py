@@ -47,7 +47,7 @@ def test_solve_vs_reference_kernel(ref_gpu, oracle, cuda, L):
     d = torch.from_numpy(np.random.default_rng(L).normal(size=(nrhs, n))).to(cuda)
     ref = d.clone()
     RefSolver(ref_gpu, oracle, n, nrhs, COMPACT, cuda).solve(ref)
-    precs = (("fp64", 1e-13), ("fp32_refine", 1e-12)) if n <= 1024 else (("fp64", 1e-13),)
+    precs = (("fp64", 1e-13), ("fp32_refine", 1e-12))
     for prec, tol in precs:
         x = d.clone()
         with ntk.Plan(n, nrhs, COMPACT, precision=prec) as p:

@@ -218,3 +218,17 @@ def test_refine_w_tuning(cuda, oracle, w):
         p.solve(t)
         torch.cuda.synchronize()
     assert oracle.rel_err(t.cpu().numpy(), _banded(oracle, 512, co, d)) < REFINE_TOL
+
+
+# Systems longer than one warp's register tile (n > 1024): overlapping
+# 512-row windows with halos below 2^-56, in place through the plan's work
+# array; the reference's largest size (n = 2048) included.
+@pytest.mark.parametrize("cname", ["compact", "dominant", "adi2048_r05"])
+@pytest.mark.parametrize("n", [1025, 1500, 2048, 4096])
+def test_refine_long_systems(cuda, oracle, cname, n):
+    co = COEFF_SETS[cname]
+    d = np.random.default_rng(n + len(cname)).normal(size=(9, n))
+    x = _solve(cuda, n, 9, co, d, precision="fp32_refine")
+    assert oracle.rel_err(x, _banded(oracle, n, co, d)) < REFINE_TOL
+    x32 = _solve(cuda, n, 9, co, d, precision="fp32")
+    assert oracle.rel_err(x32, _banded(oracle, n, co, d)) < 2e-5
