@@ -594,9 +594,9 @@ def profile_case(which):
     """Small launches of the hot kernels for `ncu` (no timing), each twice
     (warm-up + measured): compact derivative x on a 128 x 512 x 512 field and
     z on 512 x 256 x 256 (FP32 + refine with the launch configuration the
-    autotuner picks on GB300 for the benchmark: x W = 4, z W = 8 with two
-    systems per warp; FP64 defaults), `adi` one FP32 + refine ADI step on
-    2048^2 (six window launches), `batch` one FP32 + refine solve of the
+    autotuner picks on GB300 for the benchmark: x W = 4, y W = 8, z W = 8
+    with two systems per warp; FP64 defaults; y on the x field's shape), `adi` one FP32 + refine ADI step on
+    2048^2 (one launch per half step), `batch` one FP32 + refine solve of the
     4096-system uneven batch (two launches)."""
     import numpy as np
     import torch
@@ -605,7 +605,8 @@ def profile_case(which):
     from ntk.workloads import COMPACT_COEFFS, fourier_field, gaussians_2d, uneven_batch
 
     dev = torch.device("cuda", 0)
-    tuning = {"refine_x": {"refine_w": 4, "refine_spw": 1}, "refine_z": {"refine_w": 8, "refine_spw": 2}}
+    tuning = {"refine_x": {"refine_w": 4, "refine_spw": 1}, "refine_y": {"refine_w": 8, "refine_spw": 1},
+              "refine_z": {"refine_w": 8, "refine_spw": 2}}
     fields = {}
     for w in which:
         if w == "adi":
@@ -658,7 +659,7 @@ def main():
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the ADI and uneven-batch measurements")
     ap.add_argument("--profile-case", default=None,
-                    help="comma list of refine_x,refine_z,fp64_x,fp64_z: two launches each on ~256 MiB fields "
+                    help="comma list of refine_x,refine_y,refine_z,fp64_x,fp64_z,adi,batch: two launches each on ~256 MiB fields "
                          "(n = 512 along the solved axis), for ncu captures; prints nothing to time")
     args = ap.parse_args()
     if args.profile_case:

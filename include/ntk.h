@@ -70,8 +70,11 @@ int ntk_plan_create(ntk_plan** out, int n, long long nrhs, const double coeffs[7
  *                           (default), 1 whole-system shared tile, 2 direct
  *   NTK_TUNE_F64_THREADS    threads per block of the one-thread-per-system
  *                           FP64 kernel: 32, 64, 128 (default)
- *   NTK_TUNE_REFINE_W       warps per CTA of the FP32+refine kernel: 4 or
- *                           8 (default)
+ *   NTK_TUNE_REFINE_W       warps per CTA of the FP32+refine kernel: 4,
+ *                           8 (default) or 16 (kernel variants with one
+ *                           system per warp, n <= 512 and one sweep; the
+ *                           others, and the windowed n > 1024 kernel, run
+ *                           8)
  *   NTK_TUNE_REFINE_SPW     systems per warp of that kernel: 1 (default) or
  *                           2 (strided layouts with n in 257..512 only; a
  *                           CTA then stages twice as many adjacent systems) */

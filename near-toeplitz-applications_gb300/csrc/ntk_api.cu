@@ -224,7 +224,7 @@ int ntk_plan_set_tuning(ntk_plan* plan, int key, int value) {
       plan->tune_f64_threads = value;
       return NTK_OK;
     case NTK_TUNE_REFINE_W:
-      if (value != 4 && value != 8) break;
+      if (value != 4 && value != 8 && value != 16) break;
       plan->tune_refine_w = value;
       return NTK_OK;
     case NTK_TUNE_REFINE_SPW:

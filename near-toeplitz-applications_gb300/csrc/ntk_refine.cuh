@@ -91,6 +91,17 @@ template <int M>
 __host__ __device__ constexpr int sys_pitch() {
   return 32 * (M + 1) + 1;
 }
+// Pitch of the system tiles of a group of S strided systems (S a power of
+// two): a half-warp of the staging map below touches S systems times 16 / S
+// adjacent rows; a pitch of 16 / S (mod 16 doubles) puts those 16 eight-byte
+// words in 16 different bank pairs.  Rows within a tile keep the chunk pitch
+// M + 1, so the solves' own accesses are unaffected.
+// Unit-stride groups are copied one system per warp and keep sys_pitch
+// (measured 1-2% faster there).
+template <int M>
+__host__ __device__ constexpr int group_pitch(int S, long long es) {
+  return es == 1 ? sys_pitch<M>() : 32 * (M + 1) + (S < 16 ? 16 / S : 1);
+}
 template <int M>
 __device__ __forceinline__ int tile_off(int r) {
   return (r / M) * (M + 1) + (r % M);
@@ -232,14 +243,30 @@ template <int M>
 struct RefineOcc {
   static constexpr int value = (M <= 16) ? NTK_REFINE_OCC : 1;
 };
+// Launch bounds of refine_kernel.  "wide" variants fit 64 registers with at
+// most a few words of spill (rows per lane <= 8, or 16 rows with one system
+// per warp and at most one sweep): 32 resident warps per SM and CTAs of up to
+// 16 warps (measured on GB300 for 512-row systems: 4% faster unit-stride and
+// 6% faster strided than 24 warps at 80 registers).  Two sweeps or two
+// systems per warp spill 120-290 bytes at 64 registers and keep 80 registers
+// and CTAs of up to 8 warps.
+template <int M, int SWEEPS, int SPW>
+struct RefineShape {
+  static constexpr bool wide = (M <= 8 || (M == 16 && SPW == 1 && SWEEPS <= 1));
+  static constexpr int max_threads = wide ? 512 : 256;
+  static constexpr int min_blocks = wide ? 2 : RefineOcc<M>::value;
+};
+// A CTA stages at most 16 systems (the first warp's lanes 2s, 2s + 1 form the
+// boundary rows of system s).
+constexpr int REFINE_MAX_GROUP = 16;
 
 // Shared-memory footprint of one CTA: S padded system tiles, the class
 // tables (class_pitch4 float4s per class), and the boundary stencils'
 // inputs (3 doubles) and double-word results for rows 0 and n-1 of each
 // system.
 template <int M>
-__host__ __device__ constexpr size_t refine_smem(int S, int ncls) {
-  return (((size_t)S * sys_pitch<M>() * sizeof(double) + 15) & ~(size_t)15) +
+__host__ __device__ constexpr size_t refine_smem(int S, int ncls, long long es) {
+  return (((size_t)S * group_pitch<M>(S, es) * sizeof(double) + 15) & ~(size_t)15) +
          (size_t)ncls * class_pitch4<M>() * sizeof(float4) + (size_t)2 * S * (sizeof(float2) + 3 * sizeof(double));
 }
 
@@ -516,8 +543,8 @@ __device__ __forceinline__ int group_count(const Batch& b, long long grp, int S)
 template <int M, int SPW, bool PAD>
 __device__ __forceinline__ void refine_copy(const double* in, double* out, double* tiles, int n, const Batch& b,
                                             long long grp, int W, bool load) {
-  constexpr int P = sys_pitch<M>();
   const int S = SPW * W;
+  const int P = group_pitch<M>(S, b.es);
   const int wc = group_count(b, grp, S);
   if (b.es == 1) {
     constexpr int QSTEP = (32 / M) * (M + 1);
@@ -570,12 +597,13 @@ __device__ __forceinline__ void refine_copy(const double* in, double* out, doubl
 // of system s, lane 2s+1: row n-1) from their own small copies: one set of
 // FP64 instructions per CTA instead of one per system.
 template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY, int SPW>
-__global__ void __launch_bounds__(256, RefineOcc<M>::value)
+__global__ void __launch_bounds__(RefineShape<M, SWEEPS, SPW>::max_threads,
+                                  RefineShape<M, SWEEPS, SPW>::min_blocks)
     refine_kernel(const double* in, double* out, int n, Batch b, RefineArgs ra) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int P = sys_pitch<M>();
   const int W = blockDim.x >> 5;
   const int S = SPW * W;
+  const int P = group_pitch<M>(S, b.es);
   const int TC = ra.ncls * class_pitch4<M>();  // table float4s
   double* tiles = reinterpret_cast<double*>(smem_raw);  // [S][P]
   float4* tq = reinterpret_cast<float4*>(smem_raw + (((size_t)S * P * sizeof(double) + 15) & ~(size_t)15));
@@ -632,8 +660,13 @@ __global__ void __launch_bounds__(256, RefineOcc<M>::value)
 
 template <int M, int RHS, int SWEEPS, bool POW2, bool PAD, bool DECAY, int SPW>
 int launch_one(const double* in, double* out, int n, const Batch& b, const RefineArgs& ra, int W, cudaStream_t st) {
+  // the widest CTA this variant is compiled for
+  constexpr int WMAX = RefineShape<M, SWEEPS, SPW>::max_threads / 32 < REFINE_MAX_GROUP / SPW
+                           ? RefineShape<M, SWEEPS, SPW>::max_threads / 32
+                           : REFINE_MAX_GROUP / SPW;
+  if (W > WMAX) W = WMAX;
   const int S = SPW * W;
-  const size_t smem = refine_smem<M>(S, ra.ncls);
+  const size_t smem = refine_smem<M>(S, ra.ncls, b.es);
   auto kern = refine_kernel<M, RHS, SWEEPS, POW2, PAD, DECAY, SPW>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(refine_kernel)");

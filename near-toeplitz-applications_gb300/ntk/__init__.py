@@ -145,7 +145,7 @@ class Plan:
         self.close()
 
     def set_tuning(self, **kw):
-        """Set launch parameters: f64_x_variant, f64_threads, refine_w."""
+        """Set launch parameters: f64_x_variant, f64_threads, refine_w, refine_spw."""
         for k, v in kw.items():
             if k not in _lib.TUNE_KEYS:
                 raise ValueError("unknown tuning key %r" % k)

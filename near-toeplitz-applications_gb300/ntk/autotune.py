@@ -9,8 +9,8 @@ cached per (device, kernel family, n, precision, layout):
                  shared tile (threads per system = 1 in both)
   f64_threads    threads per block of the one-thread-per-system FP64 kernel
                  (systems per block for the strided sweeps)
-  refine_w       warps per CTA of the FP32 + refinement kernel
-                 (threads per system = 32, rows per lane = n / 32 in registers)
+  refine_w       warps per CTA of the FP32 + refinement kernel (4, 8, 16;
+                 threads per system = 32, rows per lane = n / 32 in registers)
   refine_spw     systems per warp (2 stages twice as many adjacent systems
                  per CTA: wider row segments for strided y/z sweeps)
 
@@ -28,9 +28,11 @@ _lock = threading.Lock()
 
 SPACE = {
     "fp64": {"f64_x_variant": [0, 1], "f64_threads": [64, 128]},
-    "fp32": {"refine_w": [4, 8], "refine_spw": [1, 2]},
-    "fp32_refine": {"refine_w": [4, 8], "refine_spw": [1, 2]},
+    "fp32": {"refine_w": [4, 8, 16], "refine_spw": [1, 2]},
+    "fp32_refine": {"refine_w": [4, 8, 16], "refine_spw": [1, 2]},
 }
+# a refinement CTA stages at most 16 systems (refine_w * refine_spw)
+MAX_GROUP = 16
 
 
 def cache_path():
@@ -70,7 +72,7 @@ def candidates(precision):
     configs = [{}]
     for name, values in space.items():
         configs = [dict(c, **{name: v}) for c in configs for v in values]
-    return configs
+    return [c for c in configs if c.get("refine_w", 1) * c.get("refine_spw", 1) <= MAX_GROUP]
 
 
 def _time(run, repeats, timer):

@@ -19,7 +19,9 @@ def test_candidates_cover_the_space():
     c = autotune.candidates("fp64")
     assert {"f64_x_variant": 0, "f64_threads": 64} in c and len(c) == 4
     c = autotune.candidates("fp32_refine")
-    assert len(c) == 4 and {"refine_w": 8, "refine_spw": 2} in c and {"refine_w": 4, "refine_spw": 1} in c
+    assert len(c) == 5 and {"refine_w": 8, "refine_spw": 2} in c and {"refine_w": 4, "refine_spw": 1} in c
+    assert {"refine_w": 16, "refine_spw": 1} in c
+    assert {"refine_w": 16, "refine_spw": 2} not in c  # more than 16 systems per CTA
 
 
 def test_tune_picks_fastest_and_caches(tmp_path, monkeypatch):
@@ -28,7 +30,7 @@ def test_tune_picks_fastest_and_caches(tmp_path, monkeypatch):
     monkeypatch.setenv("NTK_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
     monkeypatch.setattr(autotune, "device_name", lambda: "FAKE-GPU")
     plan = FakePlan("fp32_refine")
-    fake_ms = {(4, 1): 2.0, (8, 1): 1.0, (4, 2): 1.5, (8, 2): 0.5}
+    fake_ms = {(4, 1): 2.0, (8, 1): 1.0, (16, 1): 0.75, (4, 2): 1.5, (8, 2): 0.5}
     best = {"refine_w": 8, "refine_spw": 2}
 
     def timer(run, repeats):

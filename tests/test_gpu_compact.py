@@ -182,9 +182,10 @@ def test_bad_axis_extent_rejected(cuda):
 
 # Two systems per warp (a CTA stages twice as many adjacent strided
 # systems): same results on strided axes, also with padding (n = 300) and a
-# partial last group; contiguous axes ignore the setting.
+# partial last group; contiguous axes ignore the setting.  w = 16 stages 16
+# systems per CTA with one system per warp and falls back to 8 warps with two.
 @pytest.mark.parametrize("axis", [0, 1, 2])
-@pytest.mark.parametrize("n,w", [(512, 8), (300, 4), (512, 4)])
+@pytest.mark.parametrize("n,w", [(512, 8), (300, 4), (512, 4), (512, 16), (300, 16)])
 def test_refine_two_systems_per_warp(cuda, oracle, axis, n, w):
     import ntk
 

@@ -206,7 +206,7 @@ def test_fp64_x_variants(cuda, oracle, variant, n):
     assert oracle.rel_err(out.cpu().numpy(), oracle.banded_compact_deriv(f, 0.1, 2)) < FP64_TOL
 
 
-@pytest.mark.parametrize("w", [4, 8])
+@pytest.mark.parametrize("w", [4, 8, 16])
 def test_refine_w_tuning(cuda, oracle, w):
     import ntk
 
