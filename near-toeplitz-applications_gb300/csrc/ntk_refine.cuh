@@ -247,9 +247,9 @@ struct RefineOcc {
 // most a few words of spill (rows per lane <= 8, or 16 rows with one system
 // per warp and at most one sweep): 32 resident warps per SM and CTAs of up to
 // 16 warps (measured on GB300 for 512-row systems: 4% faster unit-stride and
-// 6% faster strided than 24 warps at 80 registers).  Two sweeps or two
-// systems per warp spill 120-290 bytes at 64 registers and keep 80 registers
-// and CTAs of up to 8 warps.
+// 6% faster strided than 24 warps at 80 registers).  Two sweeps spill
+// 120-290 bytes at 64 registers; two systems per warp spill 30-80 bytes there
+// and measured no faster.  Both keep 80 registers and CTAs of up to 8 warps.
 template <int M, int SWEEPS, int SPW>
 struct RefineShape {
   static constexpr bool wide = (M <= 8 || (M == 16 && SPW == 1 && SWEEPS <= 1));
