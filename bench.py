@@ -335,8 +335,11 @@ def run_gpu(args):
     # end to end through the public API: every step copies the field in from
     # pinned host memory and the three derivatives back out.  Copies and
     # solves of consecutive steps overlap on three streams (H2D, compute,
-    # D2H) with double-buffered device arrays; the timed region runs from the
-    # first H2D to the last D2H.
+    # D2H) with double-buffered device arrays; each derivative's D2H starts
+    # as soon as its axis is solved.  The timed region runs from the first
+    # H2D to the last D2H (pipeline fill included); it is taken three times
+    # and the median reported, since the host link is shared with other
+    # work on the node.
     hf = torch.empty((N, N, N), dtype=torch.float64, pin_memory=True)
     hf.copy_(f)
     houts = [torch.empty((N, N, N), dtype=torch.float64, pin_memory=True) for _ in range(3)]
@@ -358,15 +361,17 @@ def run_gpu(args):
         stream.wait_event(ev_in)
         if done_out[slot] is not None:
             stream.wait_event(done_out[slot])  # previous results of this slot are out
+        solved = []
         for axis in (2, 1, 0):
             apply(main, args.precision, axis)
             main.compact_deriv(fds[slot], ods[slot][2 - axis], axis=axis, h=h, stream=stream)
-        ev_c = torch.cuda.Event()
-        ev_c.record(stream)
-        done_comp[slot] = ev_c
+            ev_a = torch.cuda.Event()
+            ev_a.record(stream)
+            solved.append(ev_a)
+        done_comp[slot] = solved[-1]
         with torch.cuda.stream(s_out):
-            s_out.wait_event(ev_c)
             for i in range(3):
+                s_out.wait_event(solved[i])
                 houts[i].copy_(ods[slot][i], non_blocking=True)
             ev_o = torch.cuda.Event()
             ev_o.record(s_out)
@@ -376,15 +381,19 @@ def run_gpu(args):
         e2e_step(k)
     torch.cuda.synchronize(dev)
     barrier(world, dev)
-    e2e_steps = max(4, args.steps // 4)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(s_in)
-    for k in range(e2e_steps):
-        e2e_step(k)
-    e1.record(s_out)
-    torch.cuda.synchronize(dev)
-    ms_e2e = max_over_ranks(e0.elapsed_time(e1) / e2e_steps, world, dev)
+    e2e_steps = max(8, args.steps // 2)
+    e2e_runs = []
+    for _ in range(3):
+        barrier(world, dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s_in)
+        for k in range(e2e_steps):
+            e2e_step(k)
+        e1.record(s_out)
+        torch.cuda.synchronize(dev)
+        e2e_runs.append(max_over_ranks(e0.elapsed_time(e1) / e2e_steps, world, dev))
+    ms_e2e = sorted(e2e_runs)[1]
 
     if rank != 0:
         return 0
@@ -429,7 +438,10 @@ def run_gpu(args):
                          "xyz"[2 - dominant_axis], rows_launch)},
         "cpu_baseline": cpu,
         "e2e": {"value": world * ROWS_PER_STEP / (ms_e2e * 1e-3), "unit": "rows/s",
-                "h2d_bytes_per_step": 8 * N ** 3, "d2h_bytes_per_step": 3 * 8 * N ** 3},
+                "h2d_bytes_per_step": 8 * N ** 3, "d2h_bytes_per_step": 3 * 8 * N ** 3,
+                "steps": e2e_steps, "ms_per_step_runs": [round(v, 3) for v in e2e_runs],
+                "link_floor": "1 GiB in + 3 GiB out per step over the host link: 17.4 ms measured "
+                              "duplex on GB300 (23.1 G rows/s)"},
         "gpu_launches": 3 * args.steps,
         "clocks": clocks.summary(),
     }
