@@ -142,7 +142,10 @@ int ntk_transpose2d(const double* a, double* b, int N, void* stream);
 typedef struct ntk_adi ntk_adi;
 
 /* Builds the ADI solver for N x N fields (N >= 4).  precision:
- *   NTK_FP64         segmented FP64 sweeps; allocates an N x N FP64 work array.
+ *   NTK_FP64         FP64 over overlapping 32M-row windows, one warp per
+ *                    window (halos exact to FP64 rounding), when N >= 128 and
+ *                    the factors decay fast enough; otherwise segmented FP64
+ *                    sweeps with an N x N FP64 work array.
  *   NTK_FP32_REFINE  FP32 solve + one double-word refinement sweep per half
  *                    step, over overlapping 32M-row windows (M = 16, 8 or 4;
  *                    needs N >= 128, else NTK_ERR_UNSUPPORTED); matches the
@@ -153,9 +156,10 @@ int ntk_adi_create(ntk_adi** out, int N, double dx, double dt, int precision);
 
 int ntk_adi_destroy(ntk_adi* adi);
 
-/* The segmentation the plan chose: segment length, halo and segments per
- * system of the FP64 sweeps (1 segment = plain sweeps); for NTK_FP32 and
- * NTK_FP32_REFINE the windows' central rows, halo and windows per system. */
+/* The segmentation the plan chose: for windows (NTK_FP32, NTK_FP32_REFINE,
+ * and NTK_FP64 where they apply) the windows' central rows, halo and windows
+ * per system; for the segmented FP64 sweeps segment length, halo and
+ * segments per system (1 segment = plain sweeps). */
 int ntk_adi_segments(const ntk_adi* adi, int* seg_len, int* halo, int* nseg);
 
 /* One time step on device arrays u, d_x, d_y (N x N, C order), with the

@@ -12,9 +12,11 @@
 //           vertical stencil of u = d_x^T), boundary RHS = d_y's boundary
 //           columns; result written straight into u's column, which is
 //           where the reference's final transpose puts it.
-// Each half step uses the segmented FP64 sweeps (ntk_solve_f64.cu) when the
-// factors decay fast enough for the halo to be exact to rounding (r = 0.5:
-// |l| -> 0.268, a 34-row halo), giving 2046 x 8 threads instead of 2046.
+// In FP64 each half step solves overlapping windows of 32 M rows, one warp
+// per window (ntk_adi_f64.cu), when N >= 128 and the factors decay fast
+// enough for a halo exact to rounding (r = 0.5: |l| -> 0.268, 36 rows);
+// otherwise the segmented FP64 sweeps (ntk_solve_f64.cu) with the largest
+// exact segmentation.
 // A whole run of steps can be captured once in a CUDA graph and replayed.
 #include <cmath>
 #include <cstring>
@@ -22,6 +24,7 @@
 #include <tuple>
 #include <vector>
 
+#include "ntk_adi_f64.h"
 #include "ntk_adi_refine.h"
 #include "ntk_internal.h"
 #include "ntk_plan.h"
@@ -37,6 +40,7 @@ struct Adi {
   SegParams sp;
   double bottom = 0, center = 0, top = 0;
   AdiRefine* refine = nullptr;  // NTK_FP32 / NTK_FP32_REFINE half steps (ntk_adi_refine.cu)
+  AdiF64* windows = nullptr;    // NTK_FP64 window half steps (ntk_adi_f64.cu), else segmented sweeps
   cudaStream_t capture_stream = nullptr;
   std::map<std::tuple<const void*, const void*, const void*, int>, cudaGraphExec_t> graphs;
 
@@ -45,6 +49,7 @@ struct Adi {
     if (capture_stream) cudaStreamDestroy(capture_stream);
     if (scratch) cudaFree(scratch);
     if (refine) adi_refine_destroy(refine);
+    if (windows) adi_f64_destroy(windows);
   }
 };
 
@@ -56,6 +61,7 @@ namespace {
 
 int adi_step(Adi* a, double* u, double* d_x, const double* d_y, cudaStream_t st) {
   if (a->refine) return adi_refine_step(a->refine, u, d_x, d_y, st);
+  if (a->windows) return adi_f64_step(a->windows, u, d_x, d_y, st);
   const int N = a->N;
   TablesF64 t;
   t.l = a->plan.d_lw;
@@ -134,10 +140,15 @@ int ntk_adi_create(ntk_adi** out, int N, double dx, double dt, int precision) {
     std::vector<double> w(N);
     for (int i = 0; i < N; ++i) w[i] = (i < N - 1 ? a->plan.mat.c(i) : 0.0) / a->plan.lu_u[i];
     a->sp = ntk::choose_segments(a->plan.lu_l.data(), w.data(), N, N - 2);
-    if (precision == NTK_FP64)
-      rc = ntk::cuda_status(cudaMalloc(&a->scratch, sizeof(double) * (size_t)N * N), "cudaMalloc(ADI scratch)");
-    else
+    if (precision == NTK_FP64) {
+      // windows where they apply (N >= 128, fast enough decay), else the
+      // segmented sweeps with their N x N scratch array
+      rc = ntk::adi_f64_create(&a->windows, N, dx, dt);
+      if (rc == NTK_ERR_UNSUPPORTED)
+        rc = ntk::cuda_status(cudaMalloc(&a->scratch, sizeof(double) * (size_t)N * N), "cudaMalloc(ADI scratch)");
+    } else {
       rc = ntk::adi_refine_create(&a->refine, N, dx, dt, precision);
+    }
   }
   if (rc) {
     delete a;
@@ -157,10 +168,13 @@ int ntk_adi_segments(const ntk_adi* adi, int* seg_len, int* halo, int* nseg) {
     ntk::set_error("ntk_adi_segments: null plan");
     return NTK_ERR_INVALID;
   }
-  if (adi->refine) {
-    // refinement windows: central rows per window, halo, windows per system
+  if (adi->refine || adi->windows) {
+    // windows: central rows per window, halo, windows per system
     int L = 0, H = 0, P = 0;
-    ntk::adi_refine_windows(adi->refine, &L, &H, &P);
+    if (adi->refine)
+      ntk::adi_refine_windows(adi->refine, &L, &H, &P);
+    else
+      ntk::adi_f64_windows(adi->windows, &L, &H, &P);
     if (seg_len) *seg_len = L;
     if (halo) *halo = H;
     if (nseg) *nseg = P;
