@@ -608,7 +608,7 @@ def profile_case(which):
     z on 512 x 256 x 256 (FP32 + refine with the launch configuration the
     autotuner picks on GB300 for the benchmark: x W = 4, y W = 8, z W = 8
     with two systems per warp; FP64 defaults; y on the x field's shape), `adi` one FP32 + refine ADI step on
-    2048^2 (one launch per half step), `batch` one FP32 + refine solve of the
+    2048^2 (one launch per half step; `adi_f64` the same in FP64), `batch` one FP32 + refine solve of the
     4096-system uneven batch (two launches)."""
     import numpy as np
     import torch
@@ -621,12 +621,12 @@ def profile_case(which):
               "refine_z": {"refine_w": 8, "refine_spw": 2}}
     fields = {}
     for w in which:
-        if w == "adi":
+        if w in ("adi", "adi_f64"):
             NA = 2048
             dx = 1.0 / (NA - 1)
             u = gaussians_2d(NA, seed=0, device=dev)
             x, y = u.clone(), u.t().contiguous()
-            with ntk.Adi(NA, dx, dx * dx, precision="fp32_refine") as adi:
+            with ntk.Adi(NA, dx, dx * dx, precision="fp32_refine" if w == "adi" else "fp64") as adi:
                 for _ in range(2):
                     adi.step(u, x, y)
             torch.cuda.synchronize()
@@ -671,7 +671,7 @@ def main():
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the ADI and uneven-batch measurements")
     ap.add_argument("--profile-case", default=None,
-                    help="comma list of refine_x,refine_y,refine_z,fp64_x,fp64_z,adi,batch: two launches each on ~256 MiB fields "
+                    help="comma list of refine_x,refine_y,refine_z,fp64_x,fp64_z,adi,adi_f64,batch: two launches each on ~256 MiB fields "
                          "(n = 512 along the solved axis), for ncu captures; prints nothing to time")
     args = ap.parse_args()
     if args.profile_case:
