@@ -19,12 +19,16 @@
 // rows at the system's ends, (1/dx^2, -2 (1/dt + 1/dx^2), 1/dx^2) inside; the
 // right-hand side is the vertical stencil of adi/rhs.py:21-24 evaluated as
 // the segmented kernel does, fma(top, hi, fma(center, mid, bottom * lo)).
+// When the stencil's centre coefficient 2 (1/dx^2 - 1/dt) is exactly zero
+// (dt = dx^2, r = 0.5), interior rows are divided by 1/dx^2 instead: the
+// matrix becomes (1, -4, 1) and the right-hand side -(lo + hi), one FP64
+// addition instead of three operations (the solution is the same system's).
 // Window kinds (first, middle, last, whole) have their own tables, stored
 // [table][row in chunk k][lane j] so a warp's load of row k of every chunk
 // is 256 contiguous bytes.  (Folding 1/u into per-row stencil coefficients
 // saves one FP64 multiply per row but needs two more tables: measured
 // slower, and it moved the r = 40 error from below to above 1e-13.)
-// FP64 work per row: 3 (stencil) + 3 (sweeps) + 2 (carries).
+// FP64 work per row: 3 (stencil; 1 when scaled) + 3 (sweeps) + 2 (carries).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -51,7 +55,7 @@ __host__ __device__ constexpr size_t smem_bytes(int W) {
 
 // One launch per half step: CTA b solves window b / nblk of the W
 // consecutive systems starting at (b % nblk) W.  tab: [kind][NTAB][M][32].
-template <int M>
+template <int M, bool SCALED>
 __global__ void __launch_bounds__(256, 3)
     adi_f64_kernel(const double* __restrict__ in, double* __restrict__ out, AdiGeom geo,
                    const double* __restrict__ tab) {
@@ -102,8 +106,13 @@ __global__ void __launch_bounds__(256, 3)
     const double* lo = lines + (size_t)warp * P + cb;
     const double* mid = lo + P;
     const double* hi = mid + P;
+    if (SCALED) {
 #pragma unroll
-    for (int k = 0; k < M; ++k) v[k] = fma(geo.top, hi[k], fma(geo.center, mid[k], geo.bottom * lo[k]));
+      for (int k = 0; k < M; ++k) v[k] = (-lo[k]) - hi[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < M; ++k) v[k] = fma(geo.top, hi[k], fma(geo.center, mid[k], geo.bottom * lo[k]));
+    }
     // identity rows: x = the boundary value (experiments/run-adi.py:50-53)
     if ((wr.kind == 0 || wr.kind == 3) && lane == 0) v[0] = geo.bnd[s * geo.bnd_ss];
     if ((wr.kind == 2 || wr.kind == 3) && lane == 31)
@@ -166,10 +175,10 @@ __global__ void __launch_bounds__(256, 3)
   }
 }
 
-template <int M>
+template <int M, bool SCALED>
 int launch(const double* in, double* out, const AdiGeom& geo, const double* d_tab, int W, cudaStream_t st) {
   const size_t smem = smem_bytes<M>(W);
-  auto kern = adi_f64_kernel<M>;
+  auto kern = adi_f64_kernel<M, SCALED>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(adi_f64_kernel)");
   const long long blocks = (long long)geo.P * ((geo.ns + W - 1) / W);
@@ -188,6 +197,7 @@ struct AdiF64 {
   int N = 0;
   int M = 0, Lw = 0, H = 0, L = 0, P = 0;  // rows per lane, window, halo, central rows, windows
   bool whole = false;
+  bool scaled = false;         // centre coefficient 0: rows divided by 1/dx^2
   double bottom = 0.0, center = 0.0, top = 0.0;
   int wx = 4, wy = 8;          // systems per CTA: x half step (rows), y half step (columns)
   double* d_tab = nullptr;     // [4][NTAB][Lw]
@@ -239,10 +249,17 @@ int half_step(AdiF64* af, const double* in, double* out, long long is, long long
   g.bnd_ss = bnd_ss;
   g.bnd_es = bnd_es;
   using namespace adi_f64_detail;
+  if (af->scaled) {
+    switch (af->M) {
+      case 4: return launch<4, true>(in, out, g, af->d_tab, W, st);
+      case 8: return launch<8, true>(in, out, g, af->d_tab, W, st);
+      default: return launch<16, true>(in, out, g, af->d_tab, W, st);
+    }
+  }
   switch (af->M) {
-    case 4: return launch<4>(in, out, g, af->d_tab, W, st);
-    case 8: return launch<8>(in, out, g, af->d_tab, W, st);
-    default: return launch<16>(in, out, g, af->d_tab, W, st);
+    case 4: return launch<4, false>(in, out, g, af->d_tab, W, st);
+    case 8: return launch<8, false>(in, out, g, af->d_tab, W, st);
+    default: return launch<16, false>(in, out, g, af->d_tab, W, st);
   }
 }
 
@@ -302,11 +319,15 @@ int adi_f64_create(AdiF64** out, int N, double dx, double dt) {
   af->top = -e;
   af->center = 2 * (-1. / dt + e);
   // window matrices (b1, c1, ai, bi, ci, an, bn): identity rows at the
-  // system's ends, cut rows (the outside neighbour dropped) elsewhere
-  const double first[7] = {1.0, 0.0, e, b, e, e, b};
-  const double middle[7] = {b, e, e, b, e, e, b};
-  const double last[7] = {b, e, e, b, e, 0.0, 1.0};
-  const double wholem[7] = {1.0, 0.0, e, b, e, 0.0, 1.0};
+  // system's ends, cut rows (the outside neighbour dropped) elsewhere;
+  // interior rows divided by e when the stencil's centre is zero
+  af->scaled = (af->center == 0.0);
+  const double ei = af->scaled ? 1.0 : e;
+  const double bi = af->scaled ? b / e : b;
+  const double first[7] = {1.0, 0.0, ei, bi, ei, ei, bi};
+  const double middle[7] = {bi, ei, ei, bi, ei, ei, bi};
+  const double last[7] = {bi, ei, ei, bi, ei, 0.0, 1.0};
+  const double wholem[7] = {1.0, 0.0, ei, bi, ei, 0.0, 1.0};
   const double* co[4] = {first, middle, last, wholem};
   const size_t per = (size_t)adi_f64_detail::NTAB * Lw;
   std::vector<double> host(4 * per, 0.0);
