@@ -50,9 +50,10 @@ def test_golden_three_steps(cuda, oracle, golden):
 
 # FP64 paths: N = 64 segmented sweeps; 256 and 512 one whole-system window
 # (r = 40 included: slow decay, carried exactly by the lane scan); 130, 300
-# and 1000 first / middle / last windows with 36-row halos.
+# and 1000 first / middle / last windows with 36-row halos; 1024 at r = 40
+# the segmented fallback (a 276-row halo leaves no room for windows).
 @pytest.mark.parametrize("N,r,steps", [(64, 0.5, 10), (256, 0.5, 20), (256, 40.0, 5), (512, 0.5, 5),
-                                       (130, 0.5, 5), (300, 0.5, 5), (1000, 0.5, 3)])
+                                       (130, 0.5, 5), (300, 0.5, 5), (1000, 0.5, 3), (1024, 40.0, 2)])
 def test_adi_matches_oracle(cuda, oracle, N, r, steps):
     from ntk.workloads import gaussians_2d
 
