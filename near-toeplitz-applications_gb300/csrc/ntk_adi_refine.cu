@@ -39,6 +39,14 @@ namespace ntk {
 #ifndef NTK_ADI_WY
 #define NTK_ADI_WY 8
 #endif
+// launch bounds of adi_refine_kernel: CTAs of up to NTK_ADI_MAXT threads,
+// NTK_ADI_MINB of them resident per SM (80 registers for 256 x 3 or 384 x 2)
+#ifndef NTK_ADI_MAXT
+#define NTK_ADI_MAXT 256
+#endif
+#ifndef NTK_ADI_MINB
+#define NTK_ADI_MINB 3
+#endif
 
 namespace refine_detail {
 
@@ -55,7 +63,7 @@ __host__ __device__ constexpr size_t adi_smem(int W, int ncls) {
 // consecutive systems starting at (b % nblk) W; args[kind] are the window
 // kinds' kernel arguments (device memory, copied to shared memory).
 template <int M, int SWEEPS, bool POW2, bool DECAY>
-__global__ void __launch_bounds__(256, RefineOcc<M>::value)
+__global__ void __launch_bounds__(NTK_ADI_MAXT, (M <= 16) ? NTK_ADI_MINB : 1)
     adi_refine_kernel(const double* in, double* out, AdiGeom geo, const RefineArgs* args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int P = sys_pitch<M>();
