@@ -14,7 +14,11 @@
 // the converged (l, g, w).  The kernel therefore computes exactly what a
 // sequential FP64 Thomas solve with host-computed factors would.
 //
-// Work distribution.  Systems are sorted by length (longest first) and a
+// FP64 windows (batch_f64w_kernel, the default where every system admits
+// them): one warp per 512-row window, see the kernel.
+//
+// Work distribution of the one-warp-per-system kernel (batch_f64_kernel,
+// systems whose factors decay too slowly for windows).  Systems are sorted by length (longest first) and a
 // persistent grid of warps takes them from an atomic counter.  A warp splits
 // its system into up to 32 segments, one per lane, when the factors decay
 // fast enough for a halo of H rows to be exact to rounding (every halo
@@ -30,6 +34,7 @@
 #include <vector>
 
 #include "ntk_batch_refine.h"
+#include "ntk_device.cuh"
 #include "ntk_internal.h"
 #include "ntk_plan.h"
 
@@ -44,6 +49,17 @@ struct SysDesc {
   int H;          // halo
   int tab;        // offset of the head table (3K values) followed by the tail rows (6 values)
   double l_inf, g_inf, w_inf;
+};
+
+// One FP64 window (batch_f64w_kernel): system rows [w0, w0 + 512), rows
+// [lo, hi) of it written back; factors (l, g = 1/u, w = c/u) from the pool:
+// Kh head rows at `head`, the system's rows n-2, n-1 at `tail`, (cl, cg, cw)
+// elsewhere.
+struct F64Win {
+  long long off;
+  int n, w0, lo, hi;
+  int head, Kh, tail, pad_;
+  double cl, cg, cw;
 };
 
 namespace {
@@ -110,6 +126,147 @@ __global__ void __launch_bounds__(128) batch_f64_kernel(double* __restrict__ d, 
   }
 }
 
+// ---- FP64 windows: one warp per 512-row window of one system ----
+// The windows of the FP32 + refinement batch with an FP64 halo (multiplier
+// products below 2^-64): systems of up to 512 rows are one window padded
+// with identity rows; longer ones overlapping windows whose central rows are
+// written back.  Lane j holds window rows [16j, 16j+16) in registers, runs
+// Thomas's recurrences over its chunk from zero and applies the chunks'
+// carries after an exact affine scan over the lanes (as the FP64 ADI
+// windows).  A window's factors differ from the converged interior ones
+// only in its first Kh rows (the system's head table for the first window,
+// the pivot sequence from a cut for the others, host-tabulated to the exact
+// fixed point), the system's last two rows, padding rows and a cut end (c
+// dropped); the carry responses are the running products of -l and -c/u.
+constexpr int F64W_M = 16;
+constexpr int F64W_LW = 32 * F64W_M;
+constexpr int F64W_PITCH = 32 * (F64W_M + 1) + 1;  // per-warp tile, chunk pitch M + 1
+constexpr int F64W_WARPS = 4;
+
+__device__ __forceinline__ void f64w_fac(const F64Win& w, const double* __restrict__ pool, int r, double& l,
+                                         double& g, double& c) {
+  const int i = w.w0 + r;
+  if (i >= w.n) {  // padding: identity rows
+    l = 0.0, g = 1.0, c = 0.0;
+    return;
+  }
+  if (r < w.Kh) {
+    const double* p = pool + w.head + 3 * r;
+    l = __ldg(p), g = __ldg(p + 1), c = __ldg(p + 2);
+  } else if (i >= w.n - 2) {
+    const double* p = pool + w.tail + 3 * (i - (w.n - 2));
+    l = __ldg(p), g = __ldg(p + 1), c = __ldg(p + 2);
+  } else {
+    l = w.cl, g = w.cg, c = w.cw;
+  }
+  if (r == F64W_LW - 1 && i < w.n - 1) c = 0.0;  // cut end
+}
+
+__global__ void __launch_bounds__(128, 5) batch_f64w_kernel(const double* __restrict__ work, double* __restrict__ d,
+                                                            const F64Win* __restrict__ wins, long long nwin,
+                                                            const double* __restrict__ pool) {
+  __shared__ __align__(16) double tiles[F64W_WARPS * F64W_PITCH];
+  constexpr int M = F64W_M;
+  constexpr unsigned FULL = 0xffffffffu;
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long wi = (long long)blockIdx.x * F64W_WARPS + warp;
+  if (wi >= nwin) return;  // whole warps leave; no CTA barrier follows
+  const F64Win w = wins[wi];
+  double* tile = tiles + warp * F64W_PITCH;
+  const double* src = work + w.off + w.w0;
+  // stage rows (coalesced); padding rows are zero-filled
+#pragma unroll
+  for (int q = 0; q < M; ++q) {
+    const int r = lane + 32 * q;
+    const bool ok = w.w0 + r < w.n;
+    cp_async8(tile + (r / M) * (M + 1) + (r % M), ok ? src + r : work, ok ? 8u : 0u);
+  }
+  cp_async_wait_all();
+  __syncwarp();
+  const int r0 = lane * M;
+  double v[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) v[k] = tile[lane * (M + 1) + k];
+  double l, g, c;
+  // ---- forward ----
+  f64w_fac(w, pool, r0, l, g, c);
+  double b = -l;
+#pragma unroll
+  for (int k = 1; k < M; ++k) {
+    f64w_fac(w, pool, r0 + k, l, g, c);
+    v[k] = fma(-l, v[k - 1], v[k]);
+    b *= -l;
+  }
+  {
+    double a = v[M - 1];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double ap = __shfl_up_sync(FULL, a, o);
+      const double bp = __shfl_up_sync(FULL, b, o);
+      if (lane >= o) {
+        a = fma(b, ap, a);
+        b *= bp;
+      }
+    }
+    double carry = __shfl_up_sync(FULL, a, 1);
+    if (lane == 0) carry = 0.0;
+    f64w_fac(w, pool, r0, l, g, c);
+    double phi = -l;
+    v[0] = fma(phi, carry, v[0]);
+#pragma unroll
+    for (int k = 1; k < M; ++k) {
+      f64w_fac(w, pool, r0 + k, l, g, c);
+      phi *= -l;
+      v[k] = fma(phi, carry, v[k]);
+    }
+  }
+  // ---- backward ----
+  f64w_fac(w, pool, r0 + M - 1, l, g, c);
+  v[M - 1] *= g;
+  b = -c;
+#pragma unroll
+  for (int k = M - 2; k >= 0; --k) {
+    f64w_fac(w, pool, r0 + k, l, g, c);
+    v[k] = fma(-c, v[k + 1], v[k] * g);
+    b *= -c;
+  }
+  {
+    double a = v[0];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double ap = __shfl_down_sync(FULL, a, o);
+      const double bp = __shfl_down_sync(FULL, b, o);
+      if (lane + o < 32) {
+        a = fma(b, ap, a);
+        b *= bp;
+      }
+    }
+    double carry = __shfl_down_sync(FULL, a, 1);
+    if (lane == 31) carry = 0.0;
+    f64w_fac(w, pool, r0 + M - 1, l, g, c);
+    double psi = -c;
+    v[M - 1] = fma(psi, carry, v[M - 1]);
+#pragma unroll
+    for (int k = M - 2; k >= 0; --k) {
+      f64w_fac(w, pool, r0 + k, l, g, c);
+      psi *= -c;
+      v[k] = fma(psi, carry, v[k]);
+    }
+  }
+  // ---- central rows back through the tile (coalesced) ----
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < M; ++k) tile[lane * (M + 1) + k] = v[k];
+  __syncwarp();
+  double* dst = d + w.off + w.w0;
+#pragma unroll
+  for (int q = 0; q < M; ++q) {
+    const int r = lane + 32 * q;
+    if (r >= w.lo && r < w.hi) dst[r] = tile[(r / M) * (M + 1) + (r % M)];
+  }
+}
+
 }  // namespace
 
 struct Batch_ {
@@ -126,9 +283,12 @@ struct Batch_ {
   long long max_n = 0;
   long long segmented = 0;
   BatchRefine* refine = nullptr;  // NTK_FP32 / NTK_FP32_REFINE windows (ntk_batch_refine.cu)
+  F64Win* d_wins = nullptr;       // NTK_FP64 windows (batch_f64w_kernel); null: batch_f64_kernel
+  long long nwin = 0;
 
   ~Batch_() {
     if (refine) batch_refine_destroy(refine);
+    if (d_wins) cudaFree(d_wins);
     if (d_desc) cudaFree(d_desc);
     if (d_order) cudaFree(d_order);
     if (d_pool) cudaFree(d_pool);
@@ -139,10 +299,9 @@ struct Batch_ {
 
 namespace {
 
-// Host factors of one system; returns false on a zero pivot.
-bool system_factors(int n, const double* in3, const double* h6, const double* t6, SysDesc& sd,
-                    std::vector<double>& pool) {
-  Matrix m;
+// The matrix of one system: two head rows, the interior, two tail rows (for
+// n = 3 the one tail row is the second given one).
+void system_matrix(int n, const double* in3, const double* h6, const double* t6, Matrix& m) {
   m.n = n;
   m.nh = std::min(2, n);
   m.nt = std::min(2, n - m.nh);
@@ -162,6 +321,13 @@ bool system_factors(int n, const double* in3, const double* h6, const double* t6
     m.tb[0] = t6[4];
     m.tc[0] = t6[5];
   }
+}
+
+// Host factors of one system; returns false on a zero pivot.
+bool system_factors(int n, const double* in3, const double* h6, const double* t6, SysDesc& sd,
+                    std::vector<double>& pool) {
+  Matrix m;
+  system_matrix(n, in3, h6, t6, m);
   // sequential LU, stopping at the exact fixed point of the interior
   std::vector<double> l(n, 0.0), u(n, 0.0);
   u[0] = m.b(0);
@@ -236,6 +402,102 @@ bool system_factors(int n, const double* in3, const double* h6, const double* t6
   return true;
 }
 
+// Pivot sequence of the window matrix that starts at system row w0 (a
+// dropped there): rows (l, g, w) appended to the pool until the exact
+// floating-point fixed point inside the interior; K rows, then (cl, cg, cw).
+// Returns false on a zero pivot or no fixed point within `limit` rows.
+bool cut_sequence(const Matrix& m, int w0, int limit, std::vector<double>& pool, int& K, double conv[3]) {
+  const int n = m.n;
+  double u = m.b(w0);
+  if (!(u != 0.0) || !std::isfinite(u)) return false;
+  pool.push_back(0.0);
+  pool.push_back(1.0 / u);
+  pool.push_back((w0 < n - 1 ? m.c(w0) : 0.0) / u);
+  for (int i = w0 + 1; i < n && i - w0 <= limit; ++i) {
+    const double l = m.a(i) / u;
+    const double un = m.b(i) - l * m.c(i - 1);
+    if (!(un != 0.0) || !std::isfinite(un)) return false;
+    const double w = (i < n - 1 ? m.c(i) : 0.0) / un;
+    if (i >= w0 + 3 && i < n - 2 && un == u) {
+      K = i - w0;
+      conv[0] = l, conv[1] = 1.0 / un, conv[2] = w;
+      return true;
+    }
+    pool.push_back(l);
+    pool.push_back(1.0 / un);
+    pool.push_back(w);
+    u = un;
+  }
+  return false;
+}
+
+// FP64 windows of one system (see batch_f64w_kernel), appended to `wins`;
+// false when the factors decay too slowly for 128 central rows per window.
+bool system_windows(int n, const double* in3, const double* h6, const double* t6, const SysDesc& sd,
+                    std::vector<double>& pool, std::vector<F64Win>& wins, int& count) {
+  constexpr int LW = F64W_LW;
+  F64Win base{};
+  base.off = sd.off;
+  base.n = n;
+  base.tail = sd.tab + 3 * sd.K;
+  count = 0;
+  if (n <= LW) {  // one window, padded with identity rows
+    F64Win w = base;
+    w.w0 = 0, w.lo = 0, w.hi = n;
+    w.head = sd.tab, w.Kh = sd.K;
+    w.cl = sd.l_inf, w.cg = sd.g_inf, w.cw = sd.w_inf;
+    wins.push_back(w);
+    count = 1;
+    return true;
+  }
+  if (sd.K > LW / 4) return false;
+  Matrix m;
+  system_matrix(n, in3, h6, t6, m);
+  // interior cuts share one sequence (started at row 2, the first interior row)
+  int Kc = 0;
+  double cc[3];
+  const int cut_tab = (int)pool.size();
+  if (!cut_sequence(m, 2, LW / 4, pool, Kc, cc)) return false;
+  // halo: multiplier products below 2^-64 from a cut start (forward) and
+  // before a cut end (backward, |w| converged), plus two
+  const double lim = std::ldexp(1.0, -64);
+  int hf = 0, hb = 0;
+  for (double p = 1.0; p > lim && hf < 4 * LW; ++hf)
+    p *= std::fabs(hf + 1 < Kc ? pool[cut_tab + 3 * (hf + 1)] : cc[0]);
+  for (double p = 1.0; p > lim && hb < 4 * LW; ++hb) p *= std::fabs(cc[2]);
+  const int H = (std::max(hf, hb) + 2 + 1) & ~1;
+  const int L = LW - 2 * H;
+  if (L < LW / 4) return false;
+  auto add = [&](int w0, int lo, int hi, int head, int Kh, const double* cv) {
+    F64Win w = base;
+    w.w0 = w0, w.lo = lo, w.hi = hi, w.head = head, w.Kh = Kh;
+    w.cl = cv[0], w.cg = cv[1], w.cw = cv[2];
+    wins.push_back(w);
+    ++count;
+  };
+  const double sc[3] = {sd.l_inf, sd.g_inf, sd.w_inf};
+  add(0, 0, LW - H, sd.tab, sd.K, sc);
+  int pos = LW - H;
+  const int last_w0 = n - LW;
+  const int last_lo = last_w0 + H;
+  while (pos < last_lo) {
+    const int w0 = pos - H;
+    const int hi = std::min(pos + L, last_lo);
+    add(w0, pos - w0, hi - w0, cut_tab, Kc, cc);
+    pos = hi;
+  }
+  if (last_w0 >= 2) {
+    add(last_w0, pos - last_w0, LW, cut_tab, Kc, cc);
+  } else {  // n = 513: the last window starts at a head row
+    int Kl = 0;
+    double cl[3];
+    const int tab = (int)pool.size();
+    if (!cut_sequence(m, last_w0, LW / 4, pool, Kl, cl)) return false;
+    add(last_w0, pos - last_w0, LW, tab, Kl, cl);
+  }
+  return true;
+}
+
 }  // namespace
 
 }  // namespace ntk
@@ -303,6 +565,23 @@ int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long l
         return NTK_ERR_INVALID;
       }
   }
+  // FP64: windows, one warp each, when every system admits them (else the
+  // persistent one-warp-per-system kernel)
+  std::vector<ntk::F64Win> wins;
+  if (precision == NTK_FP64) {
+    long long multi = 0;
+    bool ok = true;
+    for (long long s = 0; s < nsys && ok; ++s) {
+      int count = 0;
+      ok = ntk::system_windows(n[s], interior + 3 * s, head + 6 * s, tail + 6 * s, desc[s], pool, wins, count);
+      multi += count > 1;
+    }
+    if (ok) {
+      b->segmented = multi;
+    } else {
+      wins.clear();
+    }
+  }
   std::vector<int> order(nsys);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
@@ -328,6 +607,14 @@ int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long l
     if (!rc)
       rc = ntk::cuda_status(cudaMemcpy(b->d_pool, pool.data(), sizeof(double) * pool.size(), cudaMemcpyHostToDevice),
                             "cudaMemcpy(pool)");
+    if (!rc && !wins.empty()) {
+      b->nwin = (long long)wins.size();
+      rc = ntk::cuda_status(cudaMalloc(&b->d_wins, sizeof(ntk::F64Win) * wins.size()), "cudaMalloc(windows)");
+      if (!rc)
+        rc = ntk::cuda_status(
+            cudaMemcpy(b->d_wins, wins.data(), sizeof(ntk::F64Win) * wins.size(), cudaMemcpyHostToDevice),
+            "cudaMemcpy(windows)");
+    }
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
     b->grid = sms * 8;  // 8 CTAs of 4 warps per SM, persistent
@@ -371,6 +658,17 @@ int ntk_batch_solve(ntk_batch* b, double* d, void* stream) {
   }
   cudaStream_t st = (cudaStream_t)stream;
   if (b->refine) return ntk::batch_refine_solve(b->refine, d, b->d_scratch, b->total, st);
+  if (b->d_wins) {
+    // windows overlap: read from a copy of d
+    int rc = ntk::cuda_status(
+        cudaMemcpyAsync(b->d_scratch, d, sizeof(double) * (size_t)b->total, cudaMemcpyDeviceToDevice, st),
+        "cudaMemcpyAsync(window input copy)");
+    if (rc) return rc;
+    const long long blocks = (b->nwin + ntk::F64W_WARPS - 1) / ntk::F64W_WARPS;
+    ntk::batch_f64w_kernel<<<(unsigned)blocks, 32 * ntk::F64W_WARPS, 0, st>>>(b->d_scratch, d, b->d_wins, b->nwin,
+                                                                              b->d_pool);
+    return ntk::cuda_status(cudaGetLastError(), "batch_f64w_kernel");
+  }
   int rc = ntk::cuda_status(cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), st), "cudaMemsetAsync(counter)");
   if (rc) return rc;
   ntk::batch_f64_kernel<<<b->grid, 128, 0, st>>>(d, b->d_scratch, b->d_desc, b->d_order, b->nsys, b->d_pool,
