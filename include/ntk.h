@@ -195,7 +195,7 @@ int ntk_adi_step_static(int N, double dx, double dt, double* u, double* d_x, con
 
 /* ---- uneven batches ------------------------------------------------------
  * nsys independent near-Toeplitz systems of different lengths and
- * coefficients in one buffer, solved in place by one persistent launch.
+ * coefficients in one buffer, solved in place by one launch.
  * Generalises NearToeplitzSolver (neato.py:129-197: one matrix, one
  * power-of-two n <= 2048) to a descriptor table.  System s: n[s] >= 3 rows
  * starting at element offset[s]; interior rows (a, b, c) =
@@ -205,7 +205,9 @@ int ntk_adi_step_static(int N, double dx, double dt, double* u, double* d_x, con
 typedef struct ntk_batch ntk_batch;
 
 /* Factors every system on the host (FP64) and uploads the tables; allocates
- * a work array as large as the data buffer.  precision: NTK_FP64, or
+ * a work array as large as the data buffer.  precision: NTK_FP64 (overlapping
+ * 512-row windows, one warp each, exact to FP64 rounding, when every system's
+ * factors converge and decay fast enough; otherwise one warp per system), or
  * NTK_FP32_REFINE / NTK_FP32: systems cut into overlapping 512-row windows
  * solved in FP32 with one double-word refinement sweep (NTK_ERR_UNSUPPORTED
  * when some system's pivots decay too slowly, |a/u|, |c/u| >= 0.75).
@@ -215,12 +217,16 @@ int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long l
 
 int ntk_batch_destroy(ntk_batch* batch);
 
-/* Longest system, number of systems split over several lanes, and the
- * number of elements the data buffer must span. */
+/* Longest system, number of systems split over several windows (or, on the
+ * one-warp-per-system FP64 path, over several lanes), and the number of
+ * elements the data buffer must span. */
 int ntk_batch_info(const ntk_batch* batch, long long* max_n, long long* segmented, long long* elements);
 
-/* Solves every system in place in d (device).  One kernel launch preceded
- * by a 4-byte memset of the work counter on the same stream. */
+/* Solves every system in place in d (device), asynchronously on `stream`:
+ * windows (FP64 windows, NTK_FP32_REFINE, NTK_FP32) are one device-to-device
+ * copy of d into the work array and one launch per window class; the
+ * one-warp-per-system FP64 kernel is one launch preceded by a 4-byte memset
+ * of its work counter.  Graph-capturable. */
 int ntk_batch_solve(ntk_batch* batch, double* d, void* stream);
 
 #ifdef __cplusplus
