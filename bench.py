@@ -565,8 +565,8 @@ def secondary_configs(dev, hbm):
     cpu_s = time.perf_counter() - t0
     for prec in worst:
         ub[prec]["rel_err_vs_banded_oracle_128_systems"] = worst[prec]
-    ub.update({"workload": "4096 systems, lengths log-uniform in [32, 8192], one launch (FP64) / "
-                           "512-row windows (FP32 + refine)", "rows": total_rows,
+    ub.update({"workload": "4096 systems, lengths log-uniform in [32, 8192], 512-row windows, one warp each "
+                           "(FP64: one launch; FP32 + refine: full and padded windows)", "rows": total_rows,
                "speedup_refine_vs_fp64": ub["fp64"]["ms"] / ub["fp32_refine"]["ms"],
                "cpu_baseline": {"rows_per_s": cpu_rows / cpu_s, "cores": 1, "kind": "port",
                                 "sample": "128 systems, one scipy solve_banded each"}})
