@@ -609,7 +609,8 @@ def profile_case(which):
     autotuner picks on GB300 for the benchmark: x W = 4, y W = 8, z W = 8
     with two systems per warp; FP64 defaults; y on the x field's shape), `adi` one FP32 + refine ADI step on
     2048^2 (one launch per half step; `adi_f64` the same in FP64), `batch` one FP32 + refine solve of the
-    4096-system uneven batch (two launches)."""
+    4096-system uneven batch (two launches; `batch_f64` the FP64 windows, one
+    launch)."""
     import numpy as np
     import torch
 
@@ -631,12 +632,13 @@ def profile_case(which):
                     adi.step(u, x, y)
             torch.cuda.synchronize()
             continue
-        if w == "batch":
+        if w in ("batch", "batch_f64"):
             lengths, systems = uneven_batch(4096, 32, 8192, seed=0)
             interior = np.array([sy[0] for sy in systems])
             head = np.array([sy[1] for sy in systems])
             tail = np.array([sy[2] for sy in systems])
-            with ntk.UnevenBatch(lengths, interior, head, tail, precision="fp32_refine") as bt:
+            prec = "fp32_refine" if w == "batch" else "fp64"
+            with ntk.UnevenBatch(lengths, interior, head, tail, precision=prec) as bt:
                 t = torch.from_numpy(np.random.default_rng(1).normal(size=bt.elements)).to(dev)
                 for _ in range(2):
                     bt.solve(t)
@@ -671,7 +673,7 @@ def main():
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the ADI and uneven-batch measurements")
     ap.add_argument("--profile-case", default=None,
-                    help="comma list of refine_x,refine_y,refine_z,fp64_x,fp64_z,adi,adi_f64,batch: two launches each on ~256 MiB fields "
+                    help="comma list of refine_x,refine_y,refine_z,fp64_x,fp64_z,adi,adi_f64,batch,batch_f64: two launches each on ~256 MiB fields "
                          "(n = 512 along the solved axis), for ncu captures; prints nothing to time")
     args = ap.parse_args()
     if args.profile_case:

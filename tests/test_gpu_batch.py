@@ -67,7 +67,10 @@ def test_uneven_workload_4096(cuda, oracle):
     assert info["max_n"] <= 8192 and info["segmented"] > 0
 
 
-@pytest.mark.parametrize("n", [3, 4, 5, 31, 130, 1000, 20000])
+# FP64 windows: n <= 512 one padded window; 513 (the last window starts at
+# the second head row, its own pivot sequence), 514, 600, 1000, 20000 first /
+# middle / last windows.
+@pytest.mark.parametrize("n", [3, 4, 5, 31, 130, 512, 513, 514, 600, 1000, 20000])
 def test_single_lengths(cuda, oracle, n):
     rng = np.random.default_rng(n)
     k = 5
