@@ -201,38 +201,102 @@ def cpu_path_rate(lines_per_task, tasks, processes, reps=1):
     return rows / busy, rows, busy
 
 
+def _ref_slab_worker(conn, rank, parts):
+    """One process of the reference arm: owns the z-planes [z0, z1) and the
+    y-rows [y0, y1) of the 512^3 field; on each "step" it runs the
+    reference's CPU derivative (RHS + banded solve with every line as a
+    right-hand-side column, experiments/run-compact.py:14-28) along x and y
+    of its z-slab and along z of its y-slab, including the layout changes
+    the solve needs (the CPU counterpart of the permutes of
+    run-compact.py:67-90)."""
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    sys.path.insert(0, PKG_DIR)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
+    import oracle as O
+    from ntk.workloads import fourier_block
+
+    lo = rank * N // parts
+    hi = (rank + 1) * N // parts
+    fz = fourier_block((N, N, N), (lo, 0, 0), (hi, N, N), seed=0)   # z-slab: x and y lines
+    fy = fourier_block((N, N, N), (0, lo, 0), (N, hi, N), seed=0)   # y-slab: z lines
+    h = 1.0 / (N - 1)
+    conn.send(("ready", int(fz.size + fy.size)))
+    while True:
+        msg = conn.recv()
+        if msg != "step":
+            break
+        acc = 0.0
+        for arr, axis in ((fz, 2), (fz, 1), (fy, 0)):
+            x = O.banded_compact_deriv(arr, h, axis=axis)
+            acc += float(x.flat[0])
+        conn.send(("done", acc))
+    conn.close()
+
+
 def run_reference(args):
+    """The reference arm: the reference's CPU path for the whole 512^3
+    three-direction derivative on every host core, one process per core,
+    each owning a slab of the field; a step is one derivative of the whole
+    field along x, y and z (402,653,184 rows), timed with a wall clock around
+    the step of all processes."""
     world, rank, _ = dist_setup(args)
     if rank != 0:
         return 0
+    import multiprocessing as mp
+
     cores = os.cpu_count() or 1
-    # warm-up: one small task per process (imports, LAPACK init)
-    cpu_path_rate(64, cores, cores)
-    lines = 4096  # 4096 lines x 512 rows per task
-    times = []
-    rows_total = 0
+    parts = min(cores, N)
+    ctx = mp.get_context("spawn")
+    procs, conns = [], []
+    for r in range(parts):
+        a, b = ctx.Pipe()
+        p = ctx.Process(target=_ref_slab_worker, args=(b, r, parts), daemon=True)
+        p.start()
+        procs.append(p)
+        conns.append(a)
+    for c in conns:
+        c.recv()
+
+    def step():
+        for c in conns:
+            c.send("step")
+        for c in conns:
+            c.recv()
+
     for _ in range(args.warmup):
-        cpu_path_rate(lines, cores, cores)
+        step()
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        rate, rows, wall = cpu_path_rate(lines, cores, cores)
-        times.append(wall)
-        rows_total += rows
-    value = rows_total / sum(times)
-    ms_per_step = ROWS_PER_STEP / value * 1e3
+        step()
+    wall = time.perf_counter() - t0
+    for c in conns:
+        c.send("stop")
+    for p in procs:
+        p.join(timeout=30)
+    ms_per_step = wall / args.steps * 1e3
+    value = ROWS_PER_STEP / (wall / args.steps)
     line = {
         "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "compact4 derivative x,y,z of a 512^3 FP64 field (3 x 262144 systems, n=512)",
-                   "precision": "fp64 (LAPACK banded solve)", "sample": "%d x %d lines of 512 per step" % (cores, lines)},
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(1),
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": "rows/s", "cores": cores, "kind": "port",
-                         "sample": "%d tasks x %d systems of n=512 per step, numpy RHS + scipy solve_banded "
-                                   "(experiments/run-compact.py:14-28), %d processes" % (cores, lines, cores)},
+        "precision": "fp64 (LAPACK banded solve)",
+        "cpu_baseline": {"value": value, "unit": "rows/s", "cores": parts, "kind": "port",
+                         "sample": "the whole 512^3 field per step: x, y and z derivatives, numpy RHS + scipy "
+                                   "solve_banded (experiments/run-compact.py:14-28) with the layout changes, "
+                                   "%d processes each owning a 1/%d slab, wall clock" % (parts, parts)},
         "e2e": {"value": value, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def workload_config(world):
+    """The workload description both arms print."""
+    return {"workload": "compact4 derivative x,y,z of a 512^3 FP64 field (3 x 262144 systems, n=512)",
+            "l2": "1 GiB input > 129 MB L2 (no flush)", "parallelism": "replicas x%d" % world}
 
 
 # ---------------------------------------------------------------------------
@@ -420,10 +484,9 @@ def run_gpu(args):
         "dtype": {"fp64": "f64", "fp32": "f32 (f64 in/out)",
                   "fp32_refine": "f32 solve + double-word (2x f32) residual/accumulate, f64 in/out"}[args.precision],
         "data": "synthetic",
-        "config": {"workload": "compact4 derivative x,y,z of a 512^3 FP64 field (3 x 262144 systems, n=512)",
-                   "precision": args.precision, "refine_sweeps": args.sweeps,
-                   "l2": "1 GiB input > 129 MB L2 (no flush)", "parallelism": "replicas x%d" % world,
-                   "tuning": {"%s/%s" % (p, "xyz"[2 - a]): c for (p, a), c in tuned.items()}},
+        "config": workload_config(world),
+        "precision": args.precision, "refine_sweeps": args.sweeps,
+        "tuning": {"%s/%s" % (p, "xyz"[2 - a]): c for (p, a), c in tuned.items()},
         "fp64": {"ms_per_step": ms_fp64, "rows_per_s": world * ROWS_PER_STEP / (ms_fp64 * 1e-3),
                  "hbm_frac": (BYTES_PER_ROW * N ** 3 / (per_axis64[max(per_axis64, key=per_axis64.get)] * 1e-3) / 1e9)
                  / hbm},
@@ -471,6 +534,33 @@ def secondary_configs(dev, hbm):
     import oracle as O
 
     res = {}
+    # ---- the 2D workload: 256 x 256 field, x derivative (256 systems of 256) ----
+    from ntk.workloads import COMPACT_COEFFS, fourier_field
+
+    n0 = 256
+    h0 = 1.0 / (n0 - 1)
+    f0 = fourier_field((n0, n0), seed=0, device=dev)
+    ref0 = O.banded_compact_deriv(f0.cpu().numpy()[None], h0, axis=2)[0]
+    c0 = {"workload": "2D 256 x 256 field, x derivative (256 systems of n = 256), h = 1/255"}
+    for prec in ("fp64", "fp32_refine"):
+        with ntk.Plan(n0, 0, COMPACT_COEFFS, precision=prec) as p0:
+            o0 = torch.empty_like(f0)
+            for _ in range(5):
+                p0.compact_deriv(f0, o0, axis=1, h=h0)
+            torch.cuda.synchronize(dev)
+            reps = 200
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                p0.compact_deriv(f0, o0, axis=1, h=h0)
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ms = e0.elapsed_time(e1) / reps
+            c0[prec] = {"ms": ms, "rows_per_s": n0 * n0 / (ms * 1e-3),
+                        "rel_err_vs_banded_oracle": O.rel_err(o0.cpu().numpy(), ref0),
+                        "note": "0.5 MiB field: L2-resident and launch-bound, not an HBM measurement"}
+    res["cfg0_2d_256"] = c0
     # ---- ADI ----
     NA, steps = 2048, 100
     dx = 1.0 / (NA - 1)

@@ -90,6 +90,19 @@ int ntk_plan_get_tuning(const ntk_plan* plan, int key, int* value);
 /* Frees the plan's device tables.  Synchronous; NULL is accepted. */
 int ntk_plan_destroy(ntk_plan* plan);
 
+/* Status of the plan's solves since the last status read.  The FP32 and
+ * FP32+refine kernels cannot represent |x| >= 2^128 (nor inf or nan) in
+ * their double-word arithmetic; when a solve meets such an input it still
+ * completes, with a meaningless result, and raises NTK_STATUS_RANGE in a
+ * device status word of the plan.  This call reads that word on `stream`
+ * (after every solve issued before it on that stream), clears it, waits for
+ * the stream and stores the bits in *flags (flags may be NULL).  Returns
+ * NTK_ERR_RANGE when NTK_STATUS_RANGE is set, NTK_OK otherwise; FP64 plans
+ * always report 0.  The reference validates only n (neato.py:145); this
+ * extends its error reporting to the value range.  Synchronous. */
+#define NTK_STATUS_RANGE 1
+int ntk_plan_status(ntk_plan* plan, int* flags, void* stream);
+
 /* Solves plan->nrhs contiguous systems in place: d[s*n + k], 0 <= s < nrhs.
  * Replaces NearToeplitzSolver.solve(x_d) (neato.py:168-197); d may be a
  * pointer-offset view into a larger buffer, as in experiments/run-adi.py:65. */
@@ -156,6 +169,10 @@ int ntk_adi_create(ntk_adi** out, int N, double dx, double dt, int precision);
 
 int ntk_adi_destroy(ntk_adi* adi);
 
+/* ntk_plan_status for the ADI plan's FP32 / FP32+refine half steps (FP64
+ * plans report 0).  Synchronous. */
+int ntk_adi_status(ntk_adi* adi, int* flags, void* stream);
+
 /* The segmentation the plan chose: for windows (NTK_FP32, NTK_FP32_REFINE,
  * and NTK_FP64 where they apply) the windows' central rows, halo and windows
  * per system; for the segmented FP64 sweeps segment length, halo and
@@ -186,10 +203,13 @@ int ntk_adi_run(ntk_adi* adi, double* u, double* d_x, const double* d_y, int ste
  * doubles (~2 MiB, held by every GPU that loads the library until exit).
  * N above NTK_ADI_STATIC_MAX_N is rejected with NTK_ERR_INVALID.  Calls no
  * cudaMalloc/cudaFree.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress); make it before any stream capture.  All
+ * address (cudaGetSymbolAddress) and keeps it for the life of the process (do
+ * not reset the device between calls); make that first call before any
+ * stream capture.  All
  * calls share the array: calls that overlap on the GPU race.  The factor
- * tables are copied in on `stream` by every call (cudaMemcpyAsync from a
- * per-thread host buffer). */
+ * tables are computed on the host by every call and written into the array
+ * on `stream` by a one-block kernel that receives them by value in its
+ * parameter block (no host buffer is read after the call returns). */
 #define NTK_ADI_STATIC_MAX_N 512
 int ntk_adi_step_static(int N, double dx, double dt, double* u, double* d_x, const double* d_y, void* stream);
 
@@ -216,6 +236,10 @@ int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long l
                      const double* head, const double* tail, int precision);
 
 int ntk_batch_destroy(ntk_batch* batch);
+
+/* ntk_plan_status for an uneven batch's FP32 / FP32+refine windows (FP64
+ * batches report 0).  Synchronous. */
+int ntk_batch_status(ntk_batch* batch, int* flags, void* stream);
 
 /* Longest system, number of systems split over several windows (or, on the
  * one-warp-per-system FP64 path, over several lanes), and the number of

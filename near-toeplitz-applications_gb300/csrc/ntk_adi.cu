@@ -163,6 +163,16 @@ int ntk_adi_destroy(ntk_adi* adi) {
   return NTK_OK;
 }
 
+int ntk_adi_status(ntk_adi* adi, int* flags, void* stream) {
+  if (!adi) {
+    ntk::set_error("ntk_adi_status: null plan");
+    return NTK_ERR_INVALID;
+  }
+  std::vector<unsigned*> words;
+  ntk::adi_refine_status_words(adi->refine, words);
+  return ntk::read_clear_status(words, (cudaStream_t)stream, flags);
+}
+
 int ntk_adi_segments(const ntk_adi* adi, int* seg_len, int* halo, int* nseg) {
   if (!adi) {
     ntk::set_error("ntk_adi_segments: null plan");

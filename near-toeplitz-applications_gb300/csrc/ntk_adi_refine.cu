@@ -214,6 +214,11 @@ struct AdiRefine {
   }
 };
 
+void adi_refine_status_words(const AdiRefine* ar, std::vector<unsigned*>& out) {
+  if (!ar) return;
+  for (const Plan& w : ar->win) w.status_words(out);
+}
+
 int adi_refine_create(AdiRefine** out, int N, double dx, double dt, int precision) {
   *out = nullptr;
   AdiRefine* ar = new (std::nothrow) AdiRefine();

@@ -12,6 +12,8 @@ struct AdiRefine;
 // factors decay too slowly for the windows.
 int adi_refine_create(AdiRefine** out, int N, double dx, double dt, int precision);
 void adi_refine_destroy(AdiRefine* ar);
+// the status words of the window kernels
+void adi_refine_status_words(const AdiRefine* ar, std::vector<unsigned*>& out);
 // rows each window writes back, halo (0 for one whole-system window) and
 // windows per system
 void adi_refine_windows(const AdiRefine* ar, int* L, int* H, int* P);

@@ -14,14 +14,22 @@
 //
 // The array is shared by every call: calls that overlap on the GPU (for
 // example on two streams, or from two host threads) race on it.  It keeps the
-// last call's contents; the factor tables are re-uploaded by every call and
-// every entry of the work array that a call reads is written earlier in the
-// same call, so nothing needs clearing.
+// last call's contents; every call rewrites the factor tables on its stream
+// and every entry of the work array that a call reads is written earlier in
+// the same call, so nothing needs clearing.
+//
+// The factor tables are computed on the host (O(N), no allocation) and handed
+// to a one-block kernel by value, in its parameter block (3 N doubles, at
+// most 12 KB), which copies them into the array: the values travel with the
+// launch, so no host buffer is read after the call returns and no host-device
+// copy call is made.
 //
 // In host code the array's name is only a host-side stand-in, not a device
 // address, so the device address is looked up with cudaGetSymbolAddress, once
-// per device, by the first call made with that device current.  That first
-// call should come before any stream capture on the device.
+// per device, by the first call made with that device current, and kept for
+// the life of the process (a device reset, cudaDeviceReset included, would
+// leave it stale: do not reset a device between calls).  That first call
+// should come before any stream capture on the device.
 #include <cmath>
 #include <mutex>
 
@@ -37,6 +45,15 @@ constexpr int kMaxDevices = 64;
 __device__ __align__(256) double g_adi_static_scratch[(size_t)kMaxN * kMaxN + 3 * kMaxN];
 
 double* g_scratch_addr[kMaxDevices] = {nullptr};
+
+// The factor tables l[N], w[N], g[N] (packed at stride N), passed by value.
+struct StaticTables {
+  double v[3 * kMaxN];
+};
+
+__global__ void adi_static_tables_kernel(const __grid_constant__ StaticTables t, double* dst, int count) {
+  for (int i = threadIdx.x; i < count; i += blockDim.x) dst[i] = t.v[i];
+}
 std::mutex g_scratch_mu;
 
 int scratch_address(int dev, double** out) {
@@ -80,11 +97,12 @@ extern "C" int ntk_adi_step_static(int N, double dx, double dt, double* u, doubl
   if ((rc = scratch_address(dev, &scratch))) return rc;
 
   // Factor tables of experiments/run-adi.py:50-53's matrix, built on the host
-  // in a fixed per-thread buffer (no allocation): l, w, g with g = 1/u.
-  static thread_local double tabs[3 * kMaxN];
-  double* l = tabs;
-  double* w = tabs + N;
-  double* g = tabs + 2 * N;
+  // in the kernel-parameter struct (on the stack, no allocation): l, w, g
+  // with g = 1/u.
+  StaticTables tabs;
+  double* l = tabs.v;
+  double* w = tabs.v + N;
+  double* g = tabs.v + 2 * N;
   const double a_in = 1. / (dx * dx), b_in = -2. * (1. / dt + 1. / (dx * dx)), c_in = 1. / (dx * dx);
   // rows: 0 = (1, 0), interior = (a_in, b_in, c_in), N-1 = (0, 1)
   double u_prev = 1.0;
@@ -111,8 +129,8 @@ extern "C" int ntk_adi_step_static(int N, double dx, double dt, double* u, doubl
 
   cudaStream_t st = (cudaStream_t)stream;
   double* dtab = scratch + (size_t)kMaxN * kMaxN;
-  rc = cuda_status(cudaMemcpyAsync(dtab, tabs, sizeof(double) * 3 * (size_t)N, cudaMemcpyHostToDevice, st),
-                   "cudaMemcpyAsync(ADI static tables)");
+  adi_static_tables_kernel<<<1, 256, 0, st>>>(tabs, dtab, 3 * N);
+  rc = cuda_status(cudaGetLastError(), "adi_static_tables_kernel");
   if (rc) return rc;
   TablesF64 t;
   t.l = dtab;

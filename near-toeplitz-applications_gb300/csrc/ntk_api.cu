@@ -39,6 +39,27 @@ int cuda_status(cudaError_t e, const char* where) {
   return NTK_ERR_CUDA;
 }
 
+int read_clear_status(const std::vector<unsigned*>& words, cudaStream_t st, int* flags) {
+  unsigned acc = 0;
+  for (unsigned* w : words) {
+    if (!w) continue;
+    unsigned h = 0;
+    int rc = cuda_status(cudaMemcpyAsync(&h, w, sizeof(unsigned), cudaMemcpyDeviceToHost, st),
+                         "cudaMemcpyAsync(status word)");
+    if (!rc) rc = cuda_status(cudaMemsetAsync(w, 0, sizeof(unsigned), st), "cudaMemsetAsync(status word)");
+    if (!rc) rc = cuda_status(cudaStreamSynchronize(st), "cudaStreamSynchronize(status)");
+    if (rc) return rc;
+    acc |= h;
+  }
+  if (flags) *flags = (int)acc;
+  if (acc & STATUS_RANGE) {
+    set_error("input outside the FP32 + refinement range (|x| >= 2^128, inf or nan) in a solve since the last "
+              "status read");
+    return NTK_ERR_RANGE;
+  }
+  return NTK_OK;
+}
+
 // LU factors of the near-Toeplitz matrix; false on a zero pivot.
 bool factor_host(const Matrix& m, std::vector<double>& l, std::vector<double>& u) {
   const int n = m.n;
@@ -253,6 +274,16 @@ int ntk_plan_get_tuning(const ntk_plan* plan, int key, int* value) {
       ntk::set_error("ntk_plan_get_tuning: unknown key %d", key);
       return NTK_ERR_INVALID;
   }
+}
+
+int ntk_plan_status(ntk_plan* plan, int* flags, void* stream) {
+  if (!plan) {
+    ntk::set_error("ntk_plan_status: null plan");
+    return NTK_ERR_INVALID;
+  }
+  std::vector<unsigned*> words;
+  plan->status_words(words);
+  return ntk::read_clear_status(words, (cudaStream_t)stream, flags);
 }
 
 int ntk_plan_destroy(ntk_plan* plan) {

@@ -634,6 +634,16 @@ int ntk_batch_destroy(ntk_batch* b) {
   return NTK_OK;
 }
 
+int ntk_batch_status(ntk_batch* b, int* flags, void* stream) {
+  if (!b) {
+    ntk::set_error("ntk_batch_status: null batch");
+    return NTK_ERR_INVALID;
+  }
+  std::vector<unsigned*> words;
+  if (b->refine) ntk::batch_refine_status_words(b->refine, words);
+  return ntk::read_clear_status(words, (cudaStream_t)stream, flags);
+}
+
 int ntk_batch_info(const ntk_batch* b, long long* max_n, long long* segmented, long long* elements) {
   if (!b) {
     ntk::set_error("ntk_batch_info: null batch");

@@ -260,6 +260,10 @@ DW to_dw(double v) {
 
 }  // namespace
 
+void batch_refine_status_words(const BatchRefine* br, std::vector<unsigned*>& out) {
+  if (br && br->d_status) out.push_back(br->d_status);
+}
+
 int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const long long* offset,
                         const double* interior, const double* head, const double* tail, int precision) {
   using namespace refine_detail;

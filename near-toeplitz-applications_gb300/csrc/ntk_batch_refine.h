@@ -12,6 +12,8 @@ struct BatchRefine;
 int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const long long* offset,
                         const double* interior, const double* head, const double* tail, int precision);
 void batch_refine_destroy(BatchRefine* br);
+// the status word of the window kernels
+void batch_refine_status_words(const BatchRefine* br, std::vector<unsigned*>& out);
 long long batch_refine_windows(const BatchRefine* br);
 // in place on d (elements [0, total)); work: a device array of total doubles
 int batch_refine_solve(BatchRefine* br, double* d, double* work, long long total, cudaStream_t st);

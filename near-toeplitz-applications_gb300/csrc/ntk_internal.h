@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "../../include/ntk.h"
 
@@ -111,6 +112,16 @@ struct TablesF64 {
 
 void set_error(const char* fmt, ...);
 int cuda_status(cudaError_t e, const char* where);
+
+// Status bits the FP32 / FP32+refinement kernels raise in their device
+// status words (ntk.h NTK_STATUS_*).
+constexpr unsigned STATUS_RANGE = 1u;  // an input outside the double-word range (|x| >= 2^128, inf, nan)
+
+// Reads the device status words in `words` on stream st, clears them (both in
+// stream order) and waits for the stream; *flags = the OR of the words.
+// Returns NTK_ERR_RANGE when STATUS_RANGE is set, NTK_OK otherwise, or the
+// CUDA error of a failed copy.
+int read_clear_status(const std::vector<unsigned*>& words, cudaStream_t st, int* flags);
 
 // kernels (ntk_solve_f64.cu)
 // x_variant (contiguous systems): 0 = automatic (transposing tile ring),

@@ -240,6 +240,10 @@ struct LongRefine {
   }
 };
 
+void long_refine_status_words(const LongRefine* lr, std::vector<unsigned*>& out) {
+  for (const Plan& w : lr->win) w.status_words(out);
+}
+
 int long_refine_create(LongRefine** out, const Plan& p, int precision, int sweeps) {
   using namespace refine_detail;
   *out = nullptr;

@@ -12,6 +12,8 @@ struct LongRefine;
 // decay too slowly for 512-row windows.
 int long_refine_create(LongRefine** out, const Plan& p, int precision, int sweeps);
 void long_refine_destroy(LongRefine* lr);
+// the status words of the window plans' kernels
+void long_refine_status_words(const LongRefine* lr, std::vector<unsigned*>& out);
 // a plan's solve or compact derivative (RHS_IDENTITY / RHS_COMPACT), W warps
 // per CTA (4 or 8); in place when in and out overlap (through a work array)
 int long_refine_run(LongRefine* lr, const double* in, double* out, const Batch& b, const RhsParams& rp, double s,

@@ -87,6 +87,8 @@ struct Plan {
   int init_refine();
   int run_refine(const double* in, double* out, const Batch& b, const RhsParams& rp, double s, cudaStream_t stream);
   void release_refine();
+  // device status words of this plan's FP32 kernels (none for NTK_FP64)
+  void status_words(std::vector<unsigned*>& out) const;
 };
 
 }  // namespace ntk

@@ -155,6 +155,11 @@ int Plan::init_refine() {
   return NTK_OK;
 }
 
+void Plan::status_words(std::vector<unsigned*>& out) const {
+  if (refine && refine->d_status) out.push_back(refine->d_status);
+  if (long_refine) long_refine_status_words(long_refine, out);
+}
+
 void Plan::release_refine() {
   if (long_refine) {
     long_refine_destroy(long_refine);

@@ -159,6 +159,19 @@ class Plan:
             out[k] = v.value
         return out
 
+
+    def status(self, stream=None, raise_on_error=True):
+        """Reads and clears the device status of the FP32 / FP32+refine
+        solves issued so far (synchronous on the stream): returns the
+        NTK_STATUS_* bits; with raise_on_error, an input outside the
+        double-word range (|x| >= 2^128, inf, nan) raises NtkError with
+        status NTK_ERR_RANGE."""
+        flags = ctypes.c_int()
+        rc = load().ntk_plan_status(self._h, ctypes.byref(flags), _stream(stream, None))
+        if rc != _lib.NTK_ERR_RANGE or raise_on_error:
+            check(rc)
+        return flags.value
+
     def solve(self, d, stream=None):
         """In-place solve of nrhs contiguous systems starting at d (neato.py:168-197)."""
         ne = _available(d)
@@ -209,6 +222,19 @@ class Adi:
         L, H, P = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         check(load().ntk_adi_segments(self._h, ctypes.byref(L), ctypes.byref(H), ctypes.byref(P)))
         return L.value, H.value, P.value
+
+
+    def status(self, stream=None, raise_on_error=True):
+        """Reads and clears the device status of the FP32 / FP32+refine
+        solves issued so far (synchronous on the stream): returns the
+        NTK_STATUS_* bits; with raise_on_error, an input outside the
+        double-word range (|x| >= 2^128, inf, nan) raises NtkError with
+        status NTK_ERR_RANGE."""
+        flags = ctypes.c_int()
+        rc = load().ntk_adi_status(self._h, ctypes.byref(flags), _stream(stream, None))
+        if rc != _lib.NTK_ERR_RANGE or raise_on_error:
+            check(rc)
+        return flags.value
 
     def step(self, u, d_x, d_y, stream=None):
         check(load().ntk_adi_step(self._h, device_ptr(u), device_ptr(d_x), device_ptr(d_y), _stream(stream, u)))
@@ -267,6 +293,18 @@ class UnevenBatch:
         self.lengths = n
         self.offsets = off
         self.elements = int((off + n).max()) if len(n) else 0
+
+    def status(self, stream=None, raise_on_error=True):
+        """Reads and clears the device status of the FP32 / FP32+refine
+        solves issued so far (synchronous on the stream): returns the
+        NTK_STATUS_* bits; with raise_on_error, an input outside the
+        double-word range (|x| >= 2^128, inf, nan) raises NtkError with
+        status NTK_ERR_RANGE."""
+        flags = ctypes.c_int()
+        rc = load().ntk_batch_status(self._h, ctypes.byref(flags), _stream(stream, None))
+        if rc != _lib.NTK_ERR_RANGE or raise_on_error:
+            check(rc)
+        return flags.value
 
     def info(self):
         a, b, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()

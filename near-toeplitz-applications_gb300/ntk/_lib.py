@@ -18,6 +18,8 @@ NTK_ERR_RANGE = 4
 NTK_ERR_TIMEOUT = 5
 NTK_ERR_ALLOC = 6
 
+NTK_STATUS_RANGE = 1
+
 NTK_FP64 = 0
 NTK_FP32 = 1
 NTK_FP32_REFINE = 2
@@ -43,6 +45,7 @@ SIGNATURES = [
     ("ntk_plan_set_tuning", _i, [_vp, _i, _i]),
     ("ntk_plan_get_tuning", _i, [_vp, _i, ctypes.POINTER(_i)]),
     ("ntk_plan_destroy", _i, [_vp]),
+    ("ntk_plan_status", _i, [_vp, ctypes.POINTER(_i), _vp]),
     ("ntk_solve", _i, [_vp, _vp, _vp]),
     ("ntk_solve_strided", _i, [_vp, _vp, _vp, _ll, _ll, _ll, _ll, _ll, _vp]),
     ("ntk_compact_deriv", _i, [_vp, _vp, _vp, _i, _i, _i, _i, _d, _vp]),
@@ -52,12 +55,14 @@ SIGNATURES = [
     ("ntk_transpose2d", _i, [_vp, _vp, _i, _vp]),
     ("ntk_adi_create", _i, [ctypes.POINTER(_vp), _i, _d, _d, _i]),
     ("ntk_adi_destroy", _i, [_vp]),
+    ("ntk_adi_status", _i, [_vp, ctypes.POINTER(_i), _vp]),
     ("ntk_adi_segments", _i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     ("ntk_adi_step", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("ntk_adi_run", _i, [_vp, _vp, _vp, _vp, _i, _i, _vp]),
     ("ntk_adi_step_static", _i, [_i, _d, _d, _vp, _vp, _vp, _vp]),
     ("ntk_batch_create", _i, [ctypes.POINTER(_vp), _ll, _vp, _vp, _vp, _vp, _vp, _i]),
     ("ntk_batch_destroy", _i, [_vp]),
+    ("ntk_batch_status", _i, [_vp, ctypes.POINTER(_i), _vp]),
     ("ntk_batch_info", _i, [_vp, ctypes.POINTER(_ll), ctypes.POINTER(_ll), ctypes.POINTER(_ll)]),
     ("ntk_batch_solve", _i, [_vp, _vp, _vp]),
 ]

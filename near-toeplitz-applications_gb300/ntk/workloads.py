@@ -42,6 +42,22 @@ def fourier_field(shape, seed=0, modes=8, kmax=16, device="cuda", dtype=None):
     return f
 
 
+def fourier_block(shape, lo, hi, seed=0, modes=8, kmax=16):
+    """NumPy block [lo[d], hi[d]) of fourier_field(shape, seed) (same modes,
+    same grid), for host code that holds only part of a field."""
+    amps, ks, phases = fourier_modes(len(shape), seed, modes, kmax)
+    axes = [np.linspace(0, 1, s)[a:b] for s, a, b in zip(shape, lo, hi)]
+    f = np.zeros([b - a for a, b in zip(lo, hi)])
+    for a, k, p in zip(amps, ks, phases):
+        arg = 2 * math.pi * float(p)
+        for d, (kk, ax) in enumerate(zip(k, axes)):
+            view = [1] * len(shape)
+            view[d] = ax.size
+            arg = arg + (2 * math.pi * float(kk)) * ax.reshape(view)
+        f += float(a) * np.sin(arg)
+    return f
+
+
 def gaussians_2d(N, seed=0, count=16, wmin=0.02, wmax=0.1, device="cuda"):
     """Sum of `count` Gaussians, centres U(0,1)^2, widths U(wmin, wmax), with
     zero Dirichlet boundary (the ADI initial condition)."""

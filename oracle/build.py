@@ -21,7 +21,10 @@ REF_HDR = os.path.join(REF_DIR, "ref_kernels.cuh")
 ORACLE_SO = os.path.join(HERE, "libntk_oracle.so")
 REF_CPU_SO = os.path.join(REF_DIR, "libntkref_cpu.so")
 REF_GPU_SO = os.path.join(REF_DIR, "libntkref_gpu.so")
-REFERENCE_ROOT = os.environ.get("NTK_REFERENCE_ROOT", "/root/reference")
+# Root of the reference's source tree: given to build_all() or taken from
+# NTK_REFERENCE_ROOT; with neither, or where the tree is absent, only the
+# oracle and an already rendered oracle/_ref header are built.
+REFERENCE_ROOT = os.environ.get("NTK_REFERENCE_ROOT")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -47,7 +50,7 @@ def build_oracle():
 
 def render_reference():
     """Render the reference kernels when the reference tree is present."""
-    if os.path.isfile(os.path.join(REFERENCE_ROOT, "neato.py")):
+    if REFERENCE_ROOT and os.path.isfile(os.path.join(REFERENCE_ROOT, "neato.py")):
         from importlib import util
 
         spec = util.spec_from_file_location("_ntk_render_ref", os.path.join(HERE, "render_ref.py"))
@@ -75,7 +78,12 @@ def build_ref_gpu():
     return REF_GPU_SO
 
 
-def build_all():
+def build_all(reference_root=None):
+    """Builds the oracle and, when the reference tree is at reference_root
+    (or NTK_REFERENCE_ROOT), the rendered reference kernels."""
+    global REFERENCE_ROOT
+    if reference_root:
+        REFERENCE_ROOT = reference_root
     out = {"oracle": build_oracle()}
     try:
         out["ref_cpu"] = build_ref_cpu()
@@ -91,4 +99,6 @@ def build_all():
 
 
 if __name__ == "__main__":
-    print(build_all())
+    import sys
+
+    print(build_all(sys.argv[1] if len(sys.argv) > 1 else None))

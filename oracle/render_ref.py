@@ -93,7 +93,10 @@ def precompute_coefficients_from_reference(ref_root):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NTK_REFERENCE_ROOT", "")
+    if not root:
+        print("usage: render_ref.py REFERENCE_ROOT (or set NTK_REFERENCE_ROOT)")
+        sys.exit(2)
     if not os.path.isfile(os.path.join(root, "neato.py")):
         print("reference tree not found at %s; nothing rendered" % root)
         sys.exit(0)

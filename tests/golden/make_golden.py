@@ -142,4 +142,8 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NTK_REFERENCE_ROOT", "")
+    if not root:
+        print("usage: make_golden.py REFERENCE_ROOT (or set NTK_REFERENCE_ROOT)")
+        sys.exit(2)
+    main(root)

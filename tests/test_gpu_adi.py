@@ -198,3 +198,30 @@ def test_adi_refine_needs_n_128(cuda):
         ntk.Adi(64, 1.0 / 63, 1.0 / 63 ** 2, precision="fp32_refine")
     assert "128" in str(ei.value)
     assert _lib.PRECISIONS["fp32_refine"] != _lib.PRECISIONS["fp64"]
+
+
+@pytest.fixture(scope="module")
+def adi_2048_100_steps(oracle):
+    """The benchmarked ADI workload: 2048^2, r = 0.5, the seeded Gaussian
+    initial condition, 100 steps of the long-double ADI pipeline
+    (experiments/run-adi.py:59-71 with an exact Thomas solve)."""
+    from ntk.workloads import gaussians_2d
+
+    N = 2048
+    dx = 1.0 / (N - 1)
+    dt = 2 * 0.5 * dx * dx
+    u0 = gaussians_2d(N, seed=0, device="cpu").numpy()
+    ub, xb, yb = u0.copy(), u0.copy(), u0.T.copy()
+    for _ in range(100):
+        oracle.adi_step_exact(ub, xb, yb, dx, dt)
+    return u0, ub, xb, dx, dt
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL), ("fp32_refine", 1e-12)])
+def test_adi_2048_hundred_steps_in_a_graph(cuda, oracle, adi_2048_100_steps, precision, tol):
+    """The benchmark's own run (100 steps replayed as one CUDA graph) stays
+    within the tolerance of the exact pipeline over all 100 steps."""
+    u0, ub, xb, dx, dt = adi_2048_100_steps
+    u, d_x, seg = _run(cuda, u0, dx, dt, 100, precision, graph=True)
+    assert oracle.rel_err(u, ub) < tol, (precision, seg, oracle.rel_err(u, ub))
+    assert oracle.rel_err(d_x[1:-1], xb[1:-1]) < tol

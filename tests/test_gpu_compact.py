@@ -230,3 +230,28 @@ def test_refine_long_derivative(cuda, oracle, axis, n):
         torch.cuda.synchronize()
     assert oracle.rel_err(out.cpu().numpy(), ref) < REFINE_TOL
     assert oracle.rel_err(t.cpu().numpy(), ref) < REFINE_TOL
+
+
+def test_cfg0_2d_field_x_direction(cuda, oracle):
+    """The 2D workload exactly: a 256 x 256 field, derivative along x (256
+    systems of n = 256), h = 1/255, f = 8 seeded Fourier modes (amplitudes
+    N(0,1), integer wavenumbers 1-16), against the FP64 banded oracle
+    (scipy solve_banded, experiments/run-compact.py:14-28) and the reference
+    pipeline (RHS + CR restated)."""
+    import ntk
+    from ntk.workloads import fourier_field as ff
+
+    n = 256
+    h = 1.0 / (n - 1)
+    f = ff((n, n), seed=0, device=cuda)
+    fc = f.cpu().numpy()
+    banded = oracle.banded_compact_deriv(fc[None], h, axis=2)[0]
+    ref = reference_pipeline(oracle, fc[None], h, 2)[0]
+    for prec, tol in (("fp64", FP64_TOL), ("fp32_refine", REFINE_TOL)):
+        with ntk.Plan(n, 0, COMPACT, precision=prec) as p:
+            out = torch.empty_like(f)
+            p.compact_deriv(f, out, axis=1, h=h)
+            torch.cuda.synchronize()
+        x = out.cpu().numpy()
+        assert oracle.rel_err(x, banded) < tol, (prec, oracle.rel_err(x, banded))
+        assert oracle.rel_err(x, ref) < tol, (prec, oracle.rel_err(x, ref))

@@ -49,6 +49,32 @@ def test_static_step_matches_planned_step(cuda, N, r):
             assert _rel(x_b[1:-1], x_a[1:-1]) <= TOL
 
 
+def test_static_steps_match_the_oracle_across_a_time_step_change(cuda, oracle):
+    """Two static steps in a row with different time steps (r = 0.5, then
+    r = 2), checked against the long-double ADI pipeline of the oracle after
+    each call: the second call must use its own factor tables, not the ones
+    the first call left in the static array."""
+    from ntk import _lib
+    from ntk.workloads import gaussians_2d
+
+    lib = _lib.load()
+    N = 256
+    dx = 1.0 / (N - 1)
+    u0 = gaussians_2d(N, seed=11, device=cuda)
+    u, x, y = u0.clone(), u0.clone(), u0.t().contiguous()
+    ub = u0.cpu().numpy().copy()
+    xb, yb = ub.copy(), ub.T.copy()
+    stream = torch.cuda.current_stream().cuda_stream
+    for r in (0.5, 2.0):
+        dt = 2 * r * dx * dx
+        rc = lib.ntk_adi_step_static(N, dx, dt, u.data_ptr(), x.data_ptr(), y.data_ptr(), stream)
+        assert rc == 0, _lib.last_error()
+        torch.cuda.synchronize()
+        oracle.adi_step_exact(ub, xb, yb, dx, dt)
+        assert oracle.rel_err(u.cpu().numpy(), ub) <= TOL, r
+        assert oracle.rel_err(x.cpu().numpy()[1:-1], xb[1:-1]) <= TOL, r
+
+
 def test_static_step_rejects_sizes_beyond_its_array(cuda):
     from ntk import _lib
 
