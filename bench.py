@@ -708,8 +708,11 @@ def profile_case(which):
     from ntk.workloads import COMPACT_COEFFS, fourier_field, gaussians_2d, uneven_batch
 
     dev = torch.device("cuda", 0)
-    tuning = {"refine_x": {"refine_w": 4, "refine_spw": 1}, "refine_y": {"refine_w": 8, "refine_spw": 1},
-              "refine_z": {"refine_w": 8, "refine_spw": 2}}
+    tuning = {"refine_x": {"refine_kernel": 0, "refine_w": 8}, "refine_y": {"refine_kernel": 0},
+              "refine_z": {"refine_kernel": 0},
+              "chunked_x": {"refine_kernel": 1, "refine_w": 4, "refine_spw": 1},
+              "chunked_y": {"refine_kernel": 1, "refine_w": 8, "refine_spw": 1},
+              "chunked_z": {"refine_kernel": 1, "refine_w": 8, "refine_spw": 2}}
     fields = {}
     for w in which:
         if w in ("adi", "adi_f64"):
@@ -735,6 +738,7 @@ def profile_case(which):
             torch.cuda.synchronize()
             continue
         prec, ax = w.split("_")
+        prec = "refine" if prec == "chunked" else prec
         axis = {"x": 2, "y": 1, "z": 0}[ax]
         shape = (512, 256, 256) if ax == "z" else (128, 512, 512)
         if shape not in fields:
@@ -763,7 +767,8 @@ def main():
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the ADI and uneven-batch measurements")
     ap.add_argument("--profile-case", default=None,
-                    help="comma list of refine_x,refine_y,refine_z,fp64_x,fp64_z,adi,adi_f64,batch,batch_f64: two launches each on ~256 MiB fields "
+                    help="comma list of refine_x,refine_y,refine_z (paired-chunk kernels), chunked_x,chunked_y,chunked_z, "
+                         "fp64_x,fp64_z,adi,adi_f64,batch,batch_f64: two launches each on ~256 MiB fields "
                          "(n = 512 along the solved axis), for ncu captures; prints nothing to time")
     args = ap.parse_args()
     if args.profile_case:

@@ -77,12 +77,20 @@ int ntk_plan_create(ntk_plan** out, int n, long long nrhs, const double coeffs[7
  *                           8)
  *   NTK_TUNE_REFINE_SPW     systems per warp of that kernel: 1 (default) or
  *                           2 (strided layouts with n in 257..512 only; a
- *                           CTA then stages twice as many adjacent systems) */
+ *                           CTA then stages twice as many adjacent systems)
+ *   NTK_TUNE_REFINE_KERNEL  n = 512, one sweep or none: 0 (default) the
+ *                           paired-chunk kernels with TMA tiles where the
+ *                           matrix and the layout allow them (power-of-two
+ *                           interior, 16-byte aligned buffers, even
+ *                           strides), 1 the chunked kernel above.  With 0,
+ *                           NTK_TUNE_REFINE_W sets the systems per CTA of
+ *                           contiguous layouts (4, 8 or 16). */
 enum ntk_tune_key {
   NTK_TUNE_F64_X_VARIANT = 1,
   NTK_TUNE_F64_THREADS = 2,
   NTK_TUNE_REFINE_W = 3,
-  NTK_TUNE_REFINE_SPW = 4
+  NTK_TUNE_REFINE_SPW = 4,
+  NTK_TUNE_REFINE_KERNEL = 5
 };
 int ntk_plan_set_tuning(ntk_plan* plan, int key, int value);
 int ntk_plan_get_tuning(const ntk_plan* plan, int key, int* value);

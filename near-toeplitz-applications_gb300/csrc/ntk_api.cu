@@ -252,6 +252,10 @@ int ntk_plan_set_tuning(ntk_plan* plan, int key, int value) {
       if (value != 1 && value != 2) break;
       plan->tune_refine_spw = value;
       return NTK_OK;
+    case NTK_TUNE_REFINE_KERNEL:
+      if (value != 0 && value != 1) break;
+      plan->tune_refine_kernel = value;
+      return NTK_OK;
     default:
       ntk::set_error("ntk_plan_set_tuning: unknown key %d", key);
       return NTK_ERR_INVALID;
@@ -270,6 +274,7 @@ int ntk_plan_get_tuning(const ntk_plan* plan, int key, int* value) {
     case NTK_TUNE_F64_THREADS: *value = plan->tune_f64_threads; return NTK_OK;
     case NTK_TUNE_REFINE_W: *value = plan->tune_refine_w; return NTK_OK;
     case NTK_TUNE_REFINE_SPW: *value = plan->tune_refine_spw; return NTK_OK;
+    case NTK_TUNE_REFINE_KERNEL: *value = plan->tune_refine_kernel; return NTK_OK;
     default:
       ntk::set_error("ntk_plan_get_tuning: unknown key %d", key);
       return NTK_ERR_INVALID;

@@ -1,0 +1,570 @@
+// ntk_r2.cu -- the paired-chunk FP32 + refinement solve for systems of 512
+// rows (arithmetic in ntk_r2.cuh): the compact derivative and the plain
+// solve of the plans' FP32 precisions on GB300, with the tiles moved by TMA.
+//
+// Two kernels, one per layout:
+//
+//  * r2x_kernel, contiguous systems (the x derivative, ntk_solve): a CTA
+//    holds S systems, one warp per system, lane j owning rows [16j, 16j+16).
+//    One TMA load brings the S x 4 KB box into shared memory with the
+//    128-byte swizzle, so a lane reading two adjacent rows of its chunk
+//    (16 bytes) and the other lanes of its quarter-warp hit eight different
+//    16-byte bank groups; chunk carries and edge values move by shuffles.
+//  * r2s_kernel, strided systems (the y and z derivatives): a CTA holds 16
+//    adjacent systems (128 contiguous bytes per row), a dense [512][16] TMA
+//    box; thread (warp w, lane l) owns system l % 16 and chunk 2w + l / 16,
+//    so a half-warp reads one 128-byte row and the layout needs no permute
+//    and no transpose.  Chunk carries and edge values go through shared
+//    memory with CTA barriers.
+//
+// Each thread: compact RHS (one FP64 subtraction per row) split into a
+// double-word, the FP32 solve of the pure Toeplitz factors with the Woodbury
+// end corrections, the exact double-word residual, the FP32 correction
+// solve, and the FP64 output assembled with integer operations, written in
+// place into the tile; one TMA store writes the tile back.  Out-of-range
+// inputs raise a status bit; a bounded wait on the TMA barrier that runs out
+// raises another and skips the group.
+#include <cuda.h>
+
+#include <mutex>
+
+#include "ntk_internal.h"
+#include "ntk_plan.h"
+#include "ntk_r2.h"
+
+namespace ntk {
+namespace r2 {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr unsigned STATUS_TIMEOUT = 2u;
+constexpr unsigned RANGE_MAG = 1151u << 20;  // high word of 2^128
+
+// ---------------------------------------------------------------------------
+// mbarrier / TMA (cp.async.bulk.tensor) helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// Bounded wait for phase `parity` of the barrier: false when it did not
+// complete within the limit (then the caller raises STATUS_TIMEOUT).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned ok;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store(const CUtensorMap* map, int c0, int c1, int c2, int c3, const void* src) {
+  asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%1, %2, %3, %4}], [%5];" ::"l"(map),
+               "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(src))
+               : "memory");
+}
+__device__ __forceinline__ void tma_store_commit_and_wait() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ unsigned char* align1024(unsigned char* p) {
+  return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~(uintptr_t)1023);
+}
+
+// ---------------------------------------------------------------------------
+// contiguous systems
+// ---------------------------------------------------------------------------
+// Offset (in doubles) of rows 2i, 2i+1 of chunk j in a 4 KB system tile
+// written by TMA with the 128-byte swizzle: 16-byte unit i XOR (j mod 8).
+__device__ __forceinline__ int xpair(int j, int i) { return j * 16 + ((i ^ (j & 7)) << 1); }
+
+template <int RHS, int SWEEPS>
+__global__ void __launch_bounds__(512, 2)
+    r2x_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
+               const __grid_constant__ Args a, int gpp) {
+  extern __shared__ unsigned char smem_raw[];
+  double* tile = reinterpret_cast<double*>(align1024(smem_raw));
+  const int S = blockDim.x >> 5;
+  float2* bnd = reinterpret_cast<float2*>(tile + S * NROWS);  // [S][2]: rows 0 and n-1
+  uint64_t* bar = reinterpret_cast<uint64_t*>(bnd + 2 * S);
+  const int tid = threadIdx.x, warp = tid >> 5, j = tid & 31;
+  const int plane = blockIdx.x / gpp;
+  const int s0 = (blockIdx.x - plane * gpp) * S;
+  if (tid == 0) mbar_init(bar, 1);
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(bar, (unsigned)S * NROWS * 8u);
+    tma_load(tile, &tin, 0, 0, s0, plane, bar);
+  }
+  if (!mbar_wait(bar, 0)) {
+    if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
+    return;
+  }
+  const Consts& K = a.k;
+  unsigned rmax = 0;
+  if (RHS == RHS_COMPACT) {
+    // one-sided boundary stencils of the S systems, one FP64 sequence for
+    // the CTA: lane 2s -> row 0 of system s, lane 2s+1 -> row n-1
+    if (warp == 0 && (j >> 1) < S) {
+      const double* sy = tile + (j >> 1) * NROWS;
+      const bool tl = j & 1;
+      const double r0 = tl ? sy[xpair(31, 7) + 1] : sy[xpair(0, 0)];
+      const double r1 = tl ? sy[xpair(31, 7)] : sy[xpair(0, 0) + 1];
+      const double r2 = tl ? sy[xpair(31, 6) + 1] : sy[xpair(0, 1)];
+      float h, l;
+      boundary_rhs(r0, r1, r2, tl ? a.sigmaN : a.sigma0, h, l, rmax);
+      bnd[j] = make_float2(h, l);
+    }
+    __syncthreads();
+  }
+  double* sy = tile + warp * NROWS;
+  float2 v[8];
+  // ---- right-hand side, written back in place as (hi, lo) per row ----
+  if (RHS == RHS_COMPACT) {
+    const double2 q0 = *reinterpret_cast<const double2*>(sy + xpair(j, 0));
+    const double2 q7 = *reinterpret_cast<const double2*>(sy + xpair(j, 7));
+    const double fl = __shfl_up_sync(FULL, q7.y, 1);    // row 16j - 1
+    const double fr = __shfl_down_sync(FULL, q0.x, 1);  // row 16j + 16
+    double prev = fl;
+    double2 cur = q0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      double2 nxt;
+      if (i < 6) nxt = *reinterpret_cast<const double2*>(sy + xpair(j, i + 1));
+      else if (i == 6) nxt = q7;
+      else nxt = make_double2(fr, 0.0);
+      float h0, l0, h1, l1;
+      split_f64(dsub_(cur.y, prev), h0, l0, rmax);
+      split_f64(dsub_(nxt.x, cur.x), h1, l1, rmax);
+      if (i == 0 && j == 0) {
+        const float2 b = bnd[2 * warp];
+        h0 = b.x;
+        l0 = b.y;
+      }
+      if (i == 7 && j == 31) {
+        const float2 b = bnd[2 * warp + 1];
+        h1 = b.x;
+        l1 = b.y;
+      }
+      *reinterpret_cast<float4*>(sy + xpair(j, i)) = make_float4(h0, l0, h1, l1);
+      if (i < 4) {
+        v[2 * i].x = h0;
+        v[2 * i + 1].x = h1;
+      } else {
+        v[2 * i - 8].y = h0;
+        v[2 * i - 7].y = h1;
+      }
+      prev = cur.y;
+      cur = nxt;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const double2 q = *reinterpret_cast<const double2*>(sy + xpair(j, i));
+      float h0, l0, h1, l1;
+      split_f64(q.x, h0, l0, rmax);
+      split_f64(q.y, h1, l1, rmax);
+      *reinterpret_cast<float4*>(sy + xpair(j, i)) = make_float4(h0, l0, h1, l1);
+      if (i < 4) {
+        v[2 * i].x = h0;
+        v[2 * i + 1].x = h1;
+      } else {
+        v[2 * i - 8].y = h0;
+        v[2 * i - 7].y = h1;
+      }
+    }
+  }
+  // ---- FP32 solve ----
+  {
+    float CA = __shfl_up_sync(FULL, fwd_local(v, K), 1);
+    if (j == 0) CA = 0.f;
+    bwd_local(v, CA, K);
+    float XB = __shfl_down_sync(FULL, start_comb(v, K), 1);
+    if (j == 31) XB = 0.f;
+    bwd_fix(v, XB, K);
+    if (j == 0) head_fix(v, K);
+    if (j == 31) tail_fix(v, K);
+  }
+  if (SWEEPS == 0) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      double oa0, ob0, oa1, ob1;
+      out_pair0(v[2 * i], a, oa0, ob0);
+      out_pair0(v[2 * i + 1], a, oa1, ob1);
+      *reinterpret_cast<double2*>(sy + xpair(j, i)) = make_double2(oa0, oa1);
+      *reinterpret_cast<double2*>(sy + xpair(j, i + 4)) = make_double2(ob0, ob1);
+    }
+  } else {
+    // ---- residual ----
+    float xl = __shfl_up_sync(FULL, v[7].y, 1);
+    float xr = __shfl_down_sync(FULL, v[0].x, 1);
+    if (j == 0) xl = 0.f;
+    if (j == 31) xr = 0.f;
+    float2 r[8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const float4 qa = *reinterpret_cast<const float4*>(sy + xpair(j, i));
+      const float4 qb = *reinterpret_cast<const float4*>(sy + xpair(j, i + 4));
+      const int k0 = 2 * i, k1 = 2 * i + 1;
+      const float2 xm0 = (k0 == 0) ? pair(xl, v[7].x) : v[k0 - 1];
+      r[k0] = res_pair(pair(qa.x, qb.x), pair(qa.y, qb.y), xm0, v[k0], v[k0 + 1], a);
+      const float2 xp1 = (k1 == 7) ? pair(v[0].y, xr) : v[k1 + 1];
+      r[k1] = res_pair(pair(qa.z, qb.z), pair(qa.w, qb.w), v[k1 - 1], v[k1], xp1, a);
+    }
+    if (j == 0) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+        if (q < a.nh) {
+          const float2 d = reinterpret_cast<const float2*>(sy + xpair(0, 0))[q];
+          r[q].x = res_row(d.x, d.y, q == 0 ? 0.f : v[q - 1].x, v[q].x, v[q + 1].x, a.hd[q][0], a.hd[q][1],
+                           a.hd[q][2]);
+        }
+    }
+    if (j == 31) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+        if (q < a.nt) {
+          const int k = 7 - q;  // row n-1-q is B[k] of the last chunk
+          const float2 d = reinterpret_cast<const float2*>(sy + xpair(31, (8 + k) >> 1))[(8 + k) & 1];
+          const int ti = a.nt - 1 - q;
+          r[k].y = res_row(d.x, d.y, v[k - 1].y, v[k].y, q == 0 ? 0.f : v[k + 1].y, a.td[ti][0], a.td[ti][1],
+                           a.td[ti][2]);
+        }
+    }
+    // ---- FP32 correction solve ----
+    float CA = __shfl_up_sync(FULL, fwd_local(r, K), 1);
+    if (j == 0) CA = 0.f;
+    bwd_local(r, CA, K);
+    float XB = __shfl_down_sync(FULL, start_comb(r, K), 1);
+    if (j == 31) XB = 0.f;
+    bwd_fix(r, XB, K);
+    if (j == 0) head_fix(r, K);
+    if (j == 31) tail_fix(r, K);
+    // ---- s (x + delta) as FP64, in place ----
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      double oa0, ob0, oa1, ob1;
+      out_pair(v[2 * i], r[2 * i], a, oa0, ob0);
+      out_pair(v[2 * i + 1], r[2 * i + 1], a, oa1, ob1);
+      *reinterpret_cast<double2*>(sy + xpair(j, i)) = make_double2(oa0, oa1);
+      *reinterpret_cast<double2*>(sy + xpair(j, i + 4)) = make_double2(ob0, ob1);
+    }
+  }
+  if (__any_sync(FULL, rmax >= RANGE_MAG) && j == 0 && a.status) atomicOr(a.status, 1u);
+  fence_proxy_async();
+  __syncthreads();
+  if (tid == 0) {
+    tma_store(&tout, 0, 0, s0, plane, tile);
+    tma_store_commit_and_wait();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// strided systems
+// ---------------------------------------------------------------------------
+constexpr int SG = 16;  // systems per CTA (128 contiguous bytes per row)
+// exchange arrays, [chunk][system] floats each
+enum { X_E1 = 0, X_S1, X_A0, X_B0, X_B7, X_E2, X_S2, X_COUNT };
+constexpr size_t S_TILE_BYTES = (size_t)NROWS * SG * 8;
+constexpr size_t S_SMEM = 1024 + S_TILE_BYTES + (size_t)X_COUNT * CHUNKS * SG * 4 + 16;
+
+template <int RHS, int SWEEPS>
+__global__ void __launch_bounds__(512, 2)
+    r2s_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
+               const __grid_constant__ Args a, int gpp) {
+  extern __shared__ unsigned char smem_raw[];
+  double* tile = reinterpret_cast<double*>(align1024(smem_raw));  // [512][16]
+  float* xch = reinterpret_cast<float*>(tile + NROWS * SG);         // [X_COUNT][32][16]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + X_COUNT * CHUNKS * SG);
+  const int tid = threadIdx.x;
+  const int s = tid & 15;
+  const int c = tid >> 4;  // chunk: 2 warp + (lane >> 4)
+  const int r0 = ROWS * c;
+  const int plane = blockIdx.x / gpp;
+  const int x0 = (blockIdx.x - plane * gpp) * SG;
+  if (tid == 0) mbar_init(bar, 1);
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(bar, (unsigned)S_TILE_BYTES);
+    tma_load(tile, &tin, x0, 0, plane, 0, bar);
+    tma_load(tile + (NROWS / 2) * SG, &tin, x0, NROWS / 2, plane, 0, bar);
+  }
+  if (!mbar_wait(bar, 0)) {
+    if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
+    return;
+  }
+  auto X = [&](int which, int chunk) -> float& { return xch[(which * CHUNKS + chunk) * SG + s]; };
+  const Consts& K = a.k;
+  unsigned rmax = 0;
+  double* col = tile + s;  // row r of this system: col[r * SG]
+  float2 v[8];
+  if (RHS == RHS_COMPACT) {
+    const double fl = c > 0 ? col[(r0 - 1) * SG] : 0.0;
+    const double fr = c < CHUNKS - 1 ? col[(r0 + ROWS) * SG] : 0.0;
+    float bh = 0.f, bl = 0.f;
+    if (c == 0) boundary_rhs(col[0], col[SG], col[2 * SG], a.sigma0, bh, bl, rmax);
+    if (c == CHUNKS - 1)
+      boundary_rhs(col[(NROWS - 1) * SG], col[(NROWS - 2) * SG], col[(NROWS - 3) * SG], a.sigmaN, bh, bl, rmax);
+    __syncthreads();  // every halo row is read before any row is rewritten
+    double prev = fl, cur = col[r0 * SG];
+#pragma unroll
+    for (int k = 0; k < ROWS; ++k) {
+      const double nxt = (k < ROWS - 1) ? col[(r0 + k + 1) * SG] : fr;
+      float h, l;
+      split_f64(dsub_(nxt, prev), h, l, rmax);
+      if (k == 0 && c == 0) {
+        h = bh;
+        l = bl;
+      }
+      if (k == ROWS - 1 && c == CHUNKS - 1) {
+        h = bh;
+        l = bl;
+      }
+      reinterpret_cast<float2*>(col + (r0 + k) * SG)[0] = make_float2(h, l);
+      if (k < HALF) v[k].x = h;
+      else v[k - HALF].y = h;
+      prev = cur;
+      cur = nxt;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < ROWS; ++k) {
+      float h, l;
+      split_f64(col[(r0 + k) * SG], h, l, rmax);
+      reinterpret_cast<float2*>(col + (r0 + k) * SG)[0] = make_float2(h, l);
+      if (k < HALF) v[k].x = h;
+      else v[k - HALF].y = h;
+    }
+  }
+  // ---- FP32 solve ----
+  X(X_E1, c) = fwd_local(v, K);
+  __syncthreads();
+  bwd_local(v, c > 0 ? X(X_E1, c - 1) : 0.f, K);
+  const float S1 = start_comb(v, K);
+  X(X_S1, c) = S1;
+  X(X_A0, c) = v[0].x;
+  X(X_B0, c) = v[0].y;
+  X(X_B7, c) = v[7].y;
+  __syncthreads();
+  bwd_fix(v, c < CHUNKS - 1 ? X(X_S1, c + 1) : 0.f, K);
+  if (c == 0) head_fix(v, K);
+  if (c == CHUNKS - 1) tail_fix(v, K);
+  if (SWEEPS == 0) {
+#pragma unroll
+    for (int k = 0; k < HALF; ++k) {
+      double oa, ob;
+      out_pair0(v[k], a, oa, ob);
+      col[(r0 + k) * SG] = oa;
+      col[(r0 + k + HALF) * SG] = ob;
+    }
+  } else {
+    // ---- residual ----
+    const float xl = c > 0 ? left_edge(X(X_B7, c - 1), S1, K) : 0.f;
+    const float xr =
+        c < CHUNKS - 1
+            ? right_edge(X(X_A0, c + 1), X(X_B0, c + 1), c + 2 < CHUNKS ? X(X_S1, c + 2) : 0.f, K)
+            : 0.f;
+    float2 r[8];
+#pragma unroll
+    for (int k = 0; k < HALF; ++k) {
+      const float2 da = reinterpret_cast<const float2*>(col + (r0 + k) * SG)[0];
+      const float2 db = reinterpret_cast<const float2*>(col + (r0 + k + HALF) * SG)[0];
+      const float2 xm = (k == 0) ? pair(xl, v[HALF - 1].x) : v[k - 1];
+      const float2 xp = (k == HALF - 1) ? pair(v[0].y, xr) : v[k + 1];
+      r[k] = res_pair(pair(da.x, db.x), pair(da.y, db.y), xm, v[k], xp, a);
+    }
+    if (c == 0) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+        if (q < a.nh) {
+          const float2 d = reinterpret_cast<const float2*>(col + q * SG)[0];
+          r[q].x = res_row(d.x, d.y, q == 0 ? 0.f : v[q - 1].x, v[q].x, v[q + 1].x, a.hd[q][0], a.hd[q][1],
+                           a.hd[q][2]);
+        }
+    }
+    if (c == CHUNKS - 1) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+        if (q < a.nt) {
+          const int k = HALF - 1 - q;
+          const float2 d = reinterpret_cast<const float2*>(col + (r0 + HALF + k) * SG)[0];
+          const int ti = a.nt - 1 - q;
+          r[k].y = res_row(d.x, d.y, v[k - 1].y, v[k].y, q == 0 ? 0.f : v[k + 1].y, a.td[ti][0], a.td[ti][1],
+                           a.td[ti][2]);
+        }
+    }
+    // ---- FP32 correction solve ----
+    X(X_E2, c) = fwd_local(r, K);
+    __syncthreads();
+    bwd_local(r, c > 0 ? X(X_E2, c - 1) : 0.f, K);
+    X(X_S2, c) = start_comb(r, K);
+    __syncthreads();
+    bwd_fix(r, c < CHUNKS - 1 ? X(X_S2, c + 1) : 0.f, K);
+    if (c == 0) head_fix(r, K);
+    if (c == CHUNKS - 1) tail_fix(r, K);
+#pragma unroll
+    for (int k = 0; k < HALF; ++k) {
+      double oa, ob;
+      out_pair(v[k], r[k], a, oa, ob);
+      col[(r0 + k) * SG] = oa;
+      col[(r0 + k + HALF) * SG] = ob;
+    }
+  }
+  if (__any_sync(FULL, rmax >= RANGE_MAG) && (tid & 31) == 0 && a.status) atomicOr(a.status, 1u);
+  fence_proxy_async();
+  __syncthreads();
+  if (tid == 0) {
+    tma_store(&tout, x0, 0, plane, 0, tile);
+    tma_store(&tout, x0, NROWS / 2, plane, 0, tile + (NROWS / 2) * SG);
+    tma_store_commit_and_wait();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+// Rank-4 map (unused trailing dimensions of extent 1) over `base`.
+int encode(CUtensorMap* m, const double* base, const cuuint64_t dims[4], const cuuint64_t strides[3],
+           const cuuint32_t box[4], CUtensorMapSwizzle sw) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) {
+    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return NTK_ERR_UNSUPPORTED;
+  }
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<double*>(base), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return NTK_ERR_UNSUPPORTED;
+  }
+  return NTK_OK;
+}
+
+template <int RHS, int SWEEPS>
+int launch_x(const double* in, double* out, const Batch& b, const Args& a, int S, cudaStream_t st) {
+  // dims: row in chunk, chunk, system in plane, plane
+  const long long nplanes = b.nsys > b.ni ? b.nsys / b.ni : 1;
+  const long long ni = b.nsys > b.ni ? b.ni : b.nsys;
+  const cuuint64_t dims[4] = {16, 32, (cuuint64_t)ni, (cuuint64_t)nplanes};
+  const cuuint64_t strides[3] = {128, (cuuint64_t)b.is * 8, (cuuint64_t)(nplanes > 1 ? b.os : b.is * ni) * 8};
+  const cuuint32_t box[4] = {16, 32, (cuuint32_t)S, 1};
+  CUtensorMap mi, mo;
+  int rc = encode(&mi, in, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B);
+  if (!rc) rc = encode(&mo, out, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B);
+  if (rc) return rc;
+  const long long gpp = (ni + S - 1) / S;
+  const long long grid = gpp * nplanes;
+  if (grid > 0x7fffffffLL) {
+    set_error("too many systems for one launch");
+    return NTK_ERR_INVALID;
+  }
+  const size_t smem = 1024 + (size_t)S * NROWS * 8 + (size_t)2 * S * sizeof(float2) + 16;
+  auto kern = r2x_kernel<RHS, SWEEPS>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2x_kernel)");
+  kern<<<(unsigned)grid, 32 * S, smem, st>>>(mi, mo, a, (int)gpp);
+  return cuda_status(cudaGetLastError(), "r2x_kernel");
+}
+
+template <int RHS, int SWEEPS>
+int launch_s(const double* in, double* out, const Batch& b, const Args& a, cudaStream_t st) {
+  // dims: system in plane (contiguous), row, plane
+  const long long nplanes = b.nsys > b.ni ? b.nsys / b.ni : 1;
+  const long long ni = b.nsys > b.ni ? b.ni : b.nsys;
+  const cuuint64_t dims[4] = {(cuuint64_t)ni, (cuuint64_t)NROWS, (cuuint64_t)nplanes, 1};
+  const long long ps = nplanes > 1 ? b.os : b.es * NROWS;
+  const cuuint64_t strides[3] = {(cuuint64_t)b.es * 8, (cuuint64_t)ps * 8, (cuuint64_t)ps * nplanes * 8};
+  const cuuint32_t box[4] = {(cuuint32_t)SG, (cuuint32_t)(NROWS / 2), 1, 1};
+  CUtensorMap mi, mo;
+  int rc = encode(&mi, in, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if (!rc) rc = encode(&mo, out, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if (rc) return rc;
+  const long long gpp = (ni + SG - 1) / SG;
+  const long long grid = gpp * nplanes;
+  if (grid > 0x7fffffffLL) {
+    set_error("too many systems for one launch");
+    return NTK_ERR_INVALID;
+  }
+  auto kern = r2s_kernel<RHS, SWEEPS>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_SMEM);
+  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2s_kernel)");
+  kern<<<(unsigned)grid, 32 * CHUNKS / 2, S_SMEM, st>>>(mi, mo, a, (int)gpp);
+  return cuda_status(cudaGetLastError(), "r2s_kernel");
+}
+
+}  // namespace
+
+// Whether (in, out, b) fit the tensor maps; the plan falls back to the
+// chunked kernel of ntk_refine.cuh otherwise.
+bool layout_ok(const double* in, const double* out, const Batch& b) {
+  if (!aligned16(in) || !aligned16(out) || b.nsys < 1 || b.ni < 1) return false;
+  if (b.nsys > b.ni && b.nsys % b.ni != 0) return false;
+  const long long nplanes = b.nsys > b.ni ? b.nsys / b.ni : 1;
+  const long long ni = b.nsys > b.ni ? b.ni : b.nsys;
+  if (nplanes >= (1LL << 31) || ni >= (1LL << 31)) return false;
+  if (b.es == 1) {  // contiguous systems: is >= n, is and os even
+    if (b.is < NROWS || (b.is & 1)) return false;
+    if (nplanes > 1 && ((b.os & 1) || b.os < b.is * ni)) return false;
+    return true;
+  }
+  // strided systems: adjacent systems one element apart
+  if (b.is != 1 || (b.es & 1) || b.es < ni) return false;
+  if (nplanes > 1 && ((b.os & 1) || b.os < b.es * NROWS)) return false;
+  return true;
+}
+
+int launch(const double* in, double* out, const Batch& b, const Args& a, int rhs, int sweeps, int S,
+           cudaStream_t st) {
+  if (S != 4 && S != 8 && S != 16) S = 8;
+  if (b.es == 1) {
+    if (rhs == RHS_COMPACT)
+      return sweeps ? launch_x<RHS_COMPACT, 1>(in, out, b, a, S, st) : launch_x<RHS_COMPACT, 0>(in, out, b, a, S, st);
+    return sweeps ? launch_x<RHS_IDENTITY, 1>(in, out, b, a, S, st) : launch_x<RHS_IDENTITY, 0>(in, out, b, a, S, st);
+  }
+  if (rhs == RHS_COMPACT)
+    return sweeps ? launch_s<RHS_COMPACT, 1>(in, out, b, a, st) : launch_s<RHS_COMPACT, 0>(in, out, b, a, st);
+  return sweeps ? launch_s<RHS_IDENTITY, 1>(in, out, b, a, st) : launch_s<RHS_IDENTITY, 0>(in, out, b, a, st);
+}
+
+}  // namespace r2
+}  // namespace ntk

@@ -1,0 +1,18 @@
+// ntk_r2.h -- entry points of the paired-chunk solve (ntk_r2.cu) for the plan.
+#pragma once
+#include "ntk_internal.h"
+#include "ntk_r2_host.h"
+
+namespace ntk {
+namespace r2 {
+
+// Whether in, out and the batch layout fit the kernels' tensor maps
+// (16-byte aligned buffers, even strides, whole planes).
+bool layout_ok(const double* in, const double* out, const Batch& b);
+// The solve (rhs: RHS_IDENTITY or RHS_COMPACT; sweeps 0 or 1), S systems
+// per CTA for contiguous systems (4, 8 or 16).
+int launch(const double* in, double* out, const Batch& b, const Args& a, int rhs, int sweeps, int S,
+           cudaStream_t st);
+
+}  // namespace r2
+}  // namespace ntk

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "ntk_long_refine.h"
+#include "ntk_r2.h"
 #include "ntk_refine.cuh"
 
 namespace ntk {
@@ -20,6 +21,9 @@ struct RefineState {
   unsigned* d_status = nullptr;
   bool pow2 = false;
   bool decay = false;  // chunk factor products below 2^-26: one-shuffle carries
+  // n = 512: the paired-chunk solve (ntk_r2.cu) when the matrix qualifies
+  bool r2_ok = false;
+  r2::Args r2args;
 };
 
 namespace {
@@ -152,6 +156,24 @@ int Plan::init_refine() {
     dec = (pl <= lim) && (pw <= lim);
   }
   st->decay = dec;
+  if (n == r2::NROWS) {
+    r2::MatrixRows mr;
+    mr.n = n;
+    mr.nh = mat.nh;
+    mr.nt = mat.nt;
+    for (int i = 0; i < 2; ++i) {
+      mr.head[i][0] = mat.ha[i];
+      mr.head[i][1] = mat.hb[i];
+      mr.head[i][2] = mat.hc[i];
+      mr.tail[i][0] = mat.ta[i];
+      mr.tail[i][1] = mat.tb[i];
+      mr.tail[i][2] = mat.tc[i];
+    }
+    mr.ai = mat.ai;
+    mr.bi = mat.bi;
+    mr.ci = mat.ci;
+    st->r2_ok = r2::prepare(mr, &st->r2args, nullptr);
+  }
   return NTK_OK;
 }
 
@@ -193,13 +215,19 @@ int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsPar
     set_error("compact derivative needs n >= 4");
     return NTK_ERR_INVALID;
   }
+  const int sweeps_eff = (precision == NTK_FP32) ? 0 : sweeps;
+  if (refine->r2_ok && tune_refine_kernel == 0 && sweeps_eff <= 1 && r2::layout_ok(in, out, b)) {
+    r2::Args a2 = refine->r2args;
+    r2::set_scales(&a2, rp.sigma0, rp.sigmaN, s);
+    a2.status = refine->d_status;
+    return r2::launch(in, out, b, a2, rp.kind, sweeps_eff, tune_refine_w, stream);
+  }
   RefineArgs ra;
   int M = 0;
   bool p2 = false, d = false;
   int rc = refine_args(*this, rp.sigma0, rp.sigmaN, s, &ra, &M, &p2, &d);
   if (rc) return rc;
   const int W = tune_refine_w;
-  const int sweeps_eff = (precision == NTK_FP32) ? 0 : sweeps;
   // two systems per warp: strided layouts with 16 rows per lane
   const bool spw2 = (tune_refine_spw == 2) && (M == 16) && (b.es != 1);
   switch (M) {

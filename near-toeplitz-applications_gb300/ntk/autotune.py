@@ -13,6 +13,10 @@ cached per (device, kernel family, n, precision, layout):
                  threads per system = 32, rows per lane = n / 32 in registers)
   refine_spw     systems per warp (2 stages twice as many adjacent systems
                  per CTA: wider row segments for strided y/z sweeps)
+  refine_kernel  n = 512: 0 the paired-chunk TMA kernels (16 rows per
+                 thread, two 8-row halves per packed FP32x2 instruction;
+                 refine_w = systems per CTA of contiguous layouts), 1 the
+                 chunked kernel (refine_w, refine_spw as above)
 
 Usage:
     best = autotune.tune(plan, run, key)   # run() launches the workload once
@@ -27,9 +31,11 @@ import threading
 _lock = threading.Lock()
 
 SPACE = {
-    "fp64": {"f64_x_variant": [0, 1], "f64_threads": [64, 128]},
-    "fp32": {"refine_w": [4, 8, 16], "refine_spw": [1, 2]},
-    "fp32_refine": {"refine_w": [4, 8, 16], "refine_spw": [1, 2]},
+    "fp64": [{"f64_x_variant": [0, 1], "f64_threads": [64, 128]}],
+    "fp32": [{"refine_kernel": [0], "refine_w": [4, 8, 16]},
+             {"refine_kernel": [1], "refine_w": [4, 8, 16], "refine_spw": [1, 2]}],
+    "fp32_refine": [{"refine_kernel": [0], "refine_w": [4, 8, 16]},
+                    {"refine_kernel": [1], "refine_w": [4, 8, 16], "refine_spw": [1, 2]}],
 }
 # a refinement CTA stages at most 16 systems (refine_w * refine_spw)
 MAX_GROUP = 16
@@ -68,11 +74,13 @@ def cache_key(plan, key):
 
 
 def candidates(precision):
-    space = SPACE.get(precision, {})
-    configs = [{}]
-    for name, values in space.items():
-        configs = [dict(c, **{name: v}) for c in configs for v in values]
-    return [c for c in configs if c.get("refine_w", 1) * c.get("refine_spw", 1) <= MAX_GROUP]
+    out = []
+    for space in SPACE.get(precision, [{}]):
+        configs = [{}]
+        for name, values in space.items():
+            configs = [dict(c, **{name: v}) for c in configs for v in values]
+        out += [c for c in configs if c.get("refine_w", 1) * c.get("refine_spw", 1) <= MAX_GROUP]
+    return out
 
 
 def _time(run, repeats, timer):
