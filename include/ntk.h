@@ -78,11 +78,16 @@ int ntk_plan_create(ntk_plan** out, int n, long long nrhs, const double coeffs[7
  *   NTK_TUNE_REFINE_SPW     systems per warp of that kernel: 1 (default) or
  *                           2 (strided layouts with n in 257..512 only; a
  *                           CTA then stages twice as many adjacent systems)
- *   NTK_TUNE_REFINE_KERNEL  n = 512, one sweep or none: 0 (default) the
- *                           paired-chunk kernels with TMA tiles where the
- *                           matrix and the layout allow them (power-of-two
- *                           interior, 16-byte aligned buffers, even
- *                           strides), 1 the chunked kernel above.  With 0,
+ *   NTK_TUNE_REFINE_KERNEL  n = 512, one sweep or none: the paired-chunk
+ *                           kernels with TMA tiles where the matrix and the
+ *                           layout allow them (power-of-two interior,
+ *                           16-byte aligned buffers, even strides), with
+ *                           strided layouts either one 16-system group per
+ *                           CTA (2) or in persistent CTAs, one per SM, two
+ *                           groups solved while a third loads (3); 0
+ *                           (default) picks 3 for NTK_FP32 and 2 for
+ *                           NTK_FP32_REFINE (faster on GB300); 1 the
+ *                           chunked kernel above.  With 0, 2 or 3,
  *                           NTK_TUNE_REFINE_W sets the systems per CTA of
  *                           contiguous layouts (4, 8 or 16). */
 enum ntk_tune_key {

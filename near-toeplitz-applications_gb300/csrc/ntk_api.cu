@@ -253,7 +253,7 @@ int ntk_plan_set_tuning(ntk_plan* plan, int key, int value) {
       plan->tune_refine_spw = value;
       return NTK_OK;
     case NTK_TUNE_REFINE_KERNEL:
-      if (value != 0 && value != 1) break;
+      if (value < 0 || value > 3) break;
       plan->tune_refine_kernel = value;
       return NTK_OK;
     default:

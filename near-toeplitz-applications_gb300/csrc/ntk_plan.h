@@ -76,7 +76,8 @@ struct Plan {
   int tune_f64_threads = 128;  // threads per block of the one-thread-per-system FP64 kernel
   int tune_refine_w = 8;       // warps per CTA of the refinement kernel
   int tune_refine_spw = 1;     // systems per warp (2: strided layouts, 16 rows per lane)
-  int tune_refine_kernel = 0;  // n = 512: 0 paired-chunk TMA kernels where they apply, 1 chunked kernel
+  int tune_refine_kernel = 0;  // n = 512: paired-chunk TMA kernels where they apply (0: automatic, 2: one
+                               // strided group per CTA, 3: persistent strided CTAs), 1: the chunked kernel
 
   int init(int n, long long nrhs, const double co[7], int precision, int sweeps);
   ~Plan();

@@ -112,7 +112,8 @@ __global__ void __launch_bounds__(512, 2)
     mbar_expect_tx(bar, (unsigned)S * NROWS * 8u);
     tma_load(tile, &tin, 0, 0, s0, plane, bar);
   }
-  if (!mbar_wait(bar, 0)) {
+  // every thread waits (bounded); the CTA gives up together if any did
+  if (!__syncthreads_and(mbar_wait(bar, 0))) {
     if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
     return;
   }
@@ -216,6 +217,28 @@ __global__ void __launch_bounds__(512, 2)
     float xr = __shfl_down_sync(FULL, v[0].x, 1);
     if (j == 0) xl = 0.f;
     if (j == 31) xr = 0.f;
+    // the special rows' residuals (patched in after the interior ones)
+    float rsp[2] = {0.f, 0.f};
+    if (j == 0) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+        if (q < a.nh) {
+          const float2 d = reinterpret_cast<const float2*>(sy + xpair(0, 0))[q];
+          rsp[q] = res_row(d.x, d.y, q == 0 ? 0.f : v[q - 1].x, v[q].x, v[q + 1].x, a.hd[q][0], a.hd[q][1],
+                           a.hd[q][2]);
+        }
+    }
+    if (j == 31) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+        if (q < a.nt) {
+          const int k = 7 - q;  // row n-1-q is B[k] of the last chunk
+          const float2 d = reinterpret_cast<const float2*>(sy + xpair(31, (8 + k) >> 1))[(8 + k) & 1];
+          const int ti = a.nt - 1 - q;
+          rsp[q] = res_row(d.x, d.y, v[k - 1].y, v[k].y, q == 0 ? 0.f : v[k + 1].y, a.td[ti][0], a.td[ti][1],
+                           a.td[ti][2]);
+        }
+    }
     float2 r[8];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -228,24 +251,12 @@ __global__ void __launch_bounds__(512, 2)
       r[k1] = res_pair(pair(qa.z, qb.z), pair(qa.w, qb.w), v[k1 - 1], v[k1], xp1, a);
     }
     if (j == 0) {
-#pragma unroll
-      for (int q = 0; q < 2; ++q)
-        if (q < a.nh) {
-          const float2 d = reinterpret_cast<const float2*>(sy + xpair(0, 0))[q];
-          r[q].x = res_row(d.x, d.y, q == 0 ? 0.f : v[q - 1].x, v[q].x, v[q + 1].x, a.hd[q][0], a.hd[q][1],
-                           a.hd[q][2]);
-        }
+      if (a.nh > 0) r[0].x = rsp[0];
+      if (a.nh > 1) r[1].x = rsp[1];
     }
     if (j == 31) {
-#pragma unroll
-      for (int q = 0; q < 2; ++q)
-        if (q < a.nt) {
-          const int k = 7 - q;  // row n-1-q is B[k] of the last chunk
-          const float2 d = reinterpret_cast<const float2*>(sy + xpair(31, (8 + k) >> 1))[(8 + k) & 1];
-          const int ti = a.nt - 1 - q;
-          r[k].y = res_row(d.x, d.y, v[k - 1].y, v[k].y, q == 0 ? 0.f : v[k + 1].y, a.td[ti][0], a.td[ti][1],
-                           a.td[ti][2]);
-        }
+      if (a.nt > 0) r[7].y = rsp[0];
+      if (a.nt > 1) r[6].y = rsp[1];
     }
     // ---- FP32 correction solve ----
     float CA = __shfl_up_sync(FULL, fwd_local(r, K), 1);
@@ -278,42 +289,53 @@ __global__ void __launch_bounds__(512, 2)
 // ---------------------------------------------------------------------------
 // strided systems
 // ---------------------------------------------------------------------------
-constexpr int SG = 16;  // systems per CTA (128 contiguous bytes per row)
+constexpr int SG = 16;  // systems per group (128 contiguous bytes per row)
 // exchange arrays, [chunk][system] floats each
 enum { X_E1 = 0, X_S1, X_A0, X_B0, X_B7, X_E2, X_S2, X_COUNT };
 constexpr size_t S_TILE_BYTES = (size_t)NROWS * SG * 8;
-constexpr size_t S_SMEM = 1024 + S_TILE_BYTES + (size_t)X_COUNT * CHUNKS * SG * 4 + 16;
+constexpr size_t S_XCH_FLOATS = (size_t)X_COUNT * CHUNKS * SG;
+constexpr size_t S_SMEM = 1024 + S_TILE_BYTES + S_XCH_FLOATS * 4 + 16;
+// the persistent kernel: two groups in compute, a third tile loading
+constexpr int P_BUFS = 3;
+constexpr size_t P_SMEM = 1024 + P_BUFS * S_TILE_BYTES + 2 * S_XCH_FLOATS * 4 + 8 * P_BUFS + 8;
 
-template <int RHS, int SWEEPS>
-__global__ void __launch_bounds__(512, 2)
-    r2s_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
-               const __grid_constant__ Args a, int gpp) {
-  extern __shared__ unsigned char smem_raw[];
-  double* tile = reinterpret_cast<double*>(align1024(smem_raw));  // [512][16]
-  float* xch = reinterpret_cast<float*>(tile + NROWS * SG);         // [X_COUNT][32][16]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + X_COUNT * CHUNKS * SG);
-  const int tid = threadIdx.x;
-  const int s = tid & 15;
-  const int c = tid >> 4;  // chunk: 2 warp + (lane >> 4)
+// CTA barrier of the 512 threads that work on one group: all of a
+// one-group CTA, or one half of a persistent CTA (named barrier 1 or 2).
+struct SyncAll {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct SyncHalf {
+  int id;
+  __device__ __forceinline__ void operator()() const { asm volatile("bar.sync %0, 512;" ::"r"(id) : "memory"); }
+  // barrier that also returns whether v holds in all 512 threads
+  __device__ __forceinline__ bool all(bool v) const {
+    unsigned r;
+    asm volatile(
+        "{ .reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.and.pred q, %2, 512, p; selp.u32 %0, 1, 0, q; }"
+        : "=r"(r)
+        : "r"((unsigned)v), "r"(id)
+        : "memory");
+    return r != 0;
+  }
+};
+
+// One group of 16 systems, solved in place in its [512][16] tile by 512
+// threads: thread t owns system t % 16 and chunk t / 16.  The first and
+// last rows of a chunk are the halo rows its neighbours read for the compact
+// RHS, so they are rewritten only after the first barrier; every other row
+// is rewritten as soon as it is formed.  Returns the thread's largest input
+// magnitude (high word) for the range check.
+template <int RHS, int SWEEPS, class SYNC>
+__device__ __forceinline__ unsigned strided_group(double* tile, float* xch, int t, const Args& a, SYNC sync) {
+  const int s = t & 15;
+  const int c = t >> 4;
   const int r0 = ROWS * c;
-  const int plane = blockIdx.x / gpp;
-  const int x0 = (blockIdx.x - plane * gpp) * SG;
-  if (tid == 0) mbar_init(bar, 1);
-  __syncthreads();
-  if (tid == 0) {
-    mbar_expect_tx(bar, (unsigned)S_TILE_BYTES);
-    tma_load(tile, &tin, x0, 0, plane, 0, bar);
-    tma_load(tile + (NROWS / 2) * SG, &tin, x0, NROWS / 2, plane, 0, bar);
-  }
-  if (!mbar_wait(bar, 0)) {
-    if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
-    return;
-  }
   auto X = [&](int which, int chunk) -> float& { return xch[(which * CHUNKS + chunk) * SG + s]; };
   const Consts& K = a.k;
   unsigned rmax = 0;
   double* col = tile + s;  // row r of this system: col[r * SG]
   float2 v[8];
+  float2 edge0 = make_float2(0.f, 0.f), edge15 = edge0;  // (hi, lo) of rows r0 and r0 + 15
   if (RHS == RHS_COMPACT) {
     const double fl = c > 0 ? col[(r0 - 1) * SG] : 0.0;
     const double fr = c < CHUNKS - 1 ? col[(r0 + ROWS) * SG] : 0.0;
@@ -321,7 +343,6 @@ __global__ void __launch_bounds__(512, 2)
     if (c == 0) boundary_rhs(col[0], col[SG], col[2 * SG], a.sigma0, bh, bl, rmax);
     if (c == CHUNKS - 1)
       boundary_rhs(col[(NROWS - 1) * SG], col[(NROWS - 2) * SG], col[(NROWS - 3) * SG], a.sigmaN, bh, bl, rmax);
-    __syncthreads();  // every halo row is read before any row is rewritten
     double prev = fl, cur = col[r0 * SG];
 #pragma unroll
     for (int k = 0; k < ROWS; ++k) {
@@ -336,7 +357,9 @@ __global__ void __launch_bounds__(512, 2)
         h = bh;
         l = bl;
       }
-      reinterpret_cast<float2*>(col + (r0 + k) * SG)[0] = make_float2(h, l);
+      if (k == 0) edge0 = make_float2(h, l);
+      else if (k == ROWS - 1) edge15 = make_float2(h, l);
+      else reinterpret_cast<float2*>(col + (r0 + k) * SG)[0] = make_float2(h, l);
       if (k < HALF) v[k].x = h;
       else v[k - HALF].y = h;
       prev = cur;
@@ -354,14 +377,18 @@ __global__ void __launch_bounds__(512, 2)
   }
   // ---- FP32 solve ----
   X(X_E1, c) = fwd_local(v, K);
-  __syncthreads();
+  sync();  // carries published; every halo row has been read
+  if (RHS == RHS_COMPACT) {
+    reinterpret_cast<float2*>(col + r0 * SG)[0] = edge0;
+    reinterpret_cast<float2*>(col + (r0 + ROWS - 1) * SG)[0] = edge15;
+  }
   bwd_local(v, c > 0 ? X(X_E1, c - 1) : 0.f, K);
   const float S1 = start_comb(v, K);
   X(X_S1, c) = S1;
   X(X_A0, c) = v[0].x;
   X(X_B0, c) = v[0].y;
   X(X_B7, c) = v[7].y;
-  __syncthreads();
+  sync();
   bwd_fix(v, c < CHUNKS - 1 ? X(X_S1, c + 1) : 0.f, K);
   if (c == 0) head_fix(v, K);
   if (c == CHUNKS - 1) tail_fix(v, K);
@@ -373,59 +400,100 @@ __global__ void __launch_bounds__(512, 2)
       col[(r0 + k) * SG] = oa;
       col[(r0 + k + HALF) * SG] = ob;
     }
-  } else {
-    // ---- residual ----
-    const float xl = c > 0 ? left_edge(X(X_B7, c - 1), S1, K) : 0.f;
-    const float xr =
-        c < CHUNKS - 1
-            ? right_edge(X(X_A0, c + 1), X(X_B0, c + 1), c + 2 < CHUNKS ? X(X_S1, c + 2) : 0.f, K)
-            : 0.f;
-    float2 r[8];
-#pragma unroll
-    for (int k = 0; k < HALF; ++k) {
-      const float2 da = reinterpret_cast<const float2*>(col + (r0 + k) * SG)[0];
-      const float2 db = reinterpret_cast<const float2*>(col + (r0 + k + HALF) * SG)[0];
-      const float2 xm = (k == 0) ? pair(xl, v[HALF - 1].x) : v[k - 1];
-      const float2 xp = (k == HALF - 1) ? pair(v[0].y, xr) : v[k + 1];
-      r[k] = res_pair(pair(da.x, db.x), pair(da.y, db.y), xm, v[k], xp, a);
-    }
-    if (c == 0) {
-#pragma unroll
-      for (int q = 0; q < 2; ++q)
-        if (q < a.nh) {
-          const float2 d = reinterpret_cast<const float2*>(col + q * SG)[0];
-          r[q].x = res_row(d.x, d.y, q == 0 ? 0.f : v[q - 1].x, v[q].x, v[q + 1].x, a.hd[q][0], a.hd[q][1],
-                           a.hd[q][2]);
-        }
-    }
-    if (c == CHUNKS - 1) {
-#pragma unroll
-      for (int q = 0; q < 2; ++q)
-        if (q < a.nt) {
-          const int k = HALF - 1 - q;
-          const float2 d = reinterpret_cast<const float2*>(col + (r0 + HALF + k) * SG)[0];
-          const int ti = a.nt - 1 - q;
-          r[k].y = res_row(d.x, d.y, v[k - 1].y, v[k].y, q == 0 ? 0.f : v[k + 1].y, a.td[ti][0], a.td[ti][1],
-                           a.td[ti][2]);
-        }
-    }
-    // ---- FP32 correction solve ----
-    X(X_E2, c) = fwd_local(r, K);
-    __syncthreads();
-    bwd_local(r, c > 0 ? X(X_E2, c - 1) : 0.f, K);
-    X(X_S2, c) = start_comb(r, K);
-    __syncthreads();
-    bwd_fix(r, c < CHUNKS - 1 ? X(X_S2, c + 1) : 0.f, K);
-    if (c == 0) head_fix(r, K);
-    if (c == CHUNKS - 1) tail_fix(r, K);
-#pragma unroll
-    for (int k = 0; k < HALF; ++k) {
-      double oa, ob;
-      out_pair(v[k], r[k], a, oa, ob);
-      col[(r0 + k) * SG] = oa;
-      col[(r0 + k + HALF) * SG] = ob;
-    }
+    return rmax;
   }
+  // ---- residual ----
+  const float xl = c > 0 ? left_edge(X(X_B7, c - 1), S1, K) : 0.f;
+  const float xr =
+      c < CHUNKS - 1 ? right_edge(X(X_A0, c + 1), X(X_B0, c + 1), c + 2 < CHUNKS ? X(X_S1, c + 2) : 0.f, K) : 0.f;
+  // the special rows' residuals (patched in after the interior ones)
+  float rsp[2] = {0.f, 0.f};
+  if (c == 0) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+      if (q < a.nh) {
+        const float2 d = reinterpret_cast<const float2*>(col + q * SG)[0];
+        rsp[q] =
+            res_row(d.x, d.y, q == 0 ? 0.f : v[q - 1].x, v[q].x, v[q + 1].x, a.hd[q][0], a.hd[q][1], a.hd[q][2]);
+      }
+  }
+  if (c == CHUNKS - 1) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+      if (q < a.nt) {
+        const int k = HALF - 1 - q;
+        const float2 d = reinterpret_cast<const float2*>(col + (r0 + HALF + k) * SG)[0];
+        const int ti = a.nt - 1 - q;
+        rsp[q] = res_row(d.x, d.y, v[k - 1].y, v[k].y, q == 0 ? 0.f : v[k + 1].y, a.td[ti][0], a.td[ti][1],
+                         a.td[ti][2]);
+      }
+  }
+  float2 r[8];
+#pragma unroll
+  for (int k = 0; k < HALF; ++k) {
+    const float2 da = reinterpret_cast<const float2*>(col + (r0 + k) * SG)[0];
+    const float2 db = reinterpret_cast<const float2*>(col + (r0 + k + HALF) * SG)[0];
+    const float2 xm = (k == 0) ? pair(xl, v[HALF - 1].x) : v[k - 1];
+    const float2 xp = (k == HALF - 1) ? pair(v[0].y, xr) : v[k + 1];
+    r[k] = res_pair(pair(da.x, db.x), pair(da.y, db.y), xm, v[k], xp, a);
+  }
+  if (c == 0) {
+    if (a.nh > 0) r[0].x = rsp[0];
+    if (a.nh > 1) r[1].x = rsp[1];
+  }
+  if (c == CHUNKS - 1) {
+    if (a.nt > 0) r[HALF - 1].y = rsp[0];
+    if (a.nt > 1) r[HALF - 2].y = rsp[1];
+  }
+  // ---- FP32 correction solve ----
+  X(X_E2, c) = fwd_local(r, K);
+  sync();
+  bwd_local(r, c > 0 ? X(X_E2, c - 1) : 0.f, K);
+  X(X_S2, c) = start_comb(r, K);
+  sync();
+  bwd_fix(r, c < CHUNKS - 1 ? X(X_S2, c + 1) : 0.f, K);
+  if (c == 0) head_fix(r, K);
+  if (c == CHUNKS - 1) tail_fix(r, K);
+#pragma unroll
+  for (int k = 0; k < HALF; ++k) {
+    double oa, ob;
+    out_pair(v[k], r[k], a, oa, ob);
+    col[(r0 + k) * SG] = oa;
+    col[(r0 + k + HALF) * SG] = ob;
+  }
+  return rmax;
+}
+
+// Group g of the strided layout: plane and first system.
+__device__ __forceinline__ void group_coords(int g, int gpp, int& x0, int& plane) {
+  plane = g / gpp;
+  x0 = (g - plane * gpp) * SG;
+}
+
+// One group per CTA.
+template <int RHS, int SWEEPS>
+__global__ void __launch_bounds__(512, 2)
+    r2s_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
+               const __grid_constant__ Args a, int gpp) {
+  extern __shared__ unsigned char smem_raw[];
+  double* tile = reinterpret_cast<double*>(align1024(smem_raw));  // [512][16]
+  float* xch = reinterpret_cast<float*>(tile + NROWS * SG);         // [X_COUNT][32][16]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + S_XCH_FLOATS);
+  const int tid = threadIdx.x;
+  int x0, plane;
+  group_coords(blockIdx.x, gpp, x0, plane);
+  if (tid == 0) mbar_init(bar, 1);
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(bar, (unsigned)S_TILE_BYTES);
+    tma_load(tile, &tin, x0, 0, plane, 0, bar);
+    tma_load(tile + (NROWS / 2) * SG, &tin, x0, NROWS / 2, plane, 0, bar);
+  }
+  if (!__syncthreads_and(mbar_wait(bar, 0))) {
+    if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
+    return;
+  }
+  const unsigned rmax = strided_group<RHS, SWEEPS>(tile, xch, tid, a, SyncAll());
   if (__any_sync(FULL, rmax >= RANGE_MAG) && (tid & 31) == 0 && a.status) atomicOr(a.status, 1u);
   fence_proxy_async();
   __syncthreads();
@@ -433,6 +501,97 @@ __global__ void __launch_bounds__(512, 2)
     tma_store(&tout, x0, 0, plane, 0, tile);
     tma_store(&tout, x0, NROWS / 2, plane, 0, tile + (NROWS / 2) * SG);
     tma_store_commit_and_wait();
+  }
+}
+
+// Persistent CTA (one per SM, 1024 threads): its groups are blockIdx.x +
+// k * gridDim.x, k = 0, 1, ...; half h (512 threads) solves k = h, h + 2, ...
+// in tile buffer k % 3.  The half that finishes group k stores it, and once
+// the store has read the tile it loads group k + 3 into the same buffer for
+// the other half, so one tile is always loading while two are in compute.
+// Each buffer's mbarrier completes once per load: load n of buffer b is
+// waited on with parity n & 1.
+__device__ __forceinline__ void load_group(double* buf, uint64_t* bar, const CUtensorMap* map, int g, int gpp) {
+  int x0, plane;
+  group_coords(g, gpp, x0, plane);
+  mbar_expect_tx(bar, (unsigned)S_TILE_BYTES);
+  tma_load(buf, map, x0, 0, plane, 0, bar);
+  tma_load(buf + (NROWS / 2) * SG, map, x0, NROWS / 2, plane, 0, bar);
+}
+
+// Layout of the persistent kernel's shared memory.
+struct PSmem {
+  double* bufs;    // [3][512][16] tiles
+  float* xch;      // [2][X_COUNT][32][16] exchange arrays
+  uint64_t* bars;  // [3] tile barriers
+  int* knext;      // [2] next group index of each half
+};
+__device__ __forceinline__ PSmem psmem() {
+  extern __shared__ unsigned char smem_raw[];
+  PSmem p;
+  p.bufs = reinterpret_cast<double*>(align1024(smem_raw));
+  p.xch = reinterpret_cast<float*>(p.bufs + P_BUFS * NROWS * SG);
+  p.bars = reinterpret_cast<uint64_t*>(p.xch + 2 * S_XCH_FLOATS);
+  p.knext = reinterpret_cast<int*>(p.bars + P_BUFS);
+  return p;
+}
+
+// Thread 0 of half h after the half's group: store it from its tile, and
+// once the store has read the tile load the group three places further on
+// into it for the other half.  Not inlined, so that nothing it needs stays
+// in registers across the group's solve.
+__device__ __noinline__ void finish_group(const CUtensorMap* tin, const CUtensorMap* tout, int gpp, int ngroups,
+                                          int h) {
+  const PSmem sm = psmem();
+  const int G = gridDim.x;
+  const int kcount = (ngroups - (int)blockIdx.x + G - 1) / G;
+  const int k = sm.knext[h] - 2;
+  const int b = k % P_BUFS;
+  double* tile = sm.bufs + (size_t)b * NROWS * SG;
+  int x0, plane;
+  group_coords(blockIdx.x + k * G, gpp, x0, plane);
+  tma_store(tout, x0, 0, plane, 0, tile);
+  tma_store(tout, x0, NROWS / 2, plane, 0, tile + (NROWS / 2) * SG);
+  tma_store_commit_and_wait();
+  if (k + P_BUFS < kcount) load_group(tile, sm.bars + b, tin, blockIdx.x + (k + P_BUFS) * G, gpp);
+}
+
+template <int RHS, int SWEEPS>
+__global__ void __launch_bounds__(1024, 1)
+    r2sp_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
+                const __grid_constant__ Args a, int gpp, int ngroups) {
+  const PSmem sm = psmem();
+  const int tid = threadIdx.x;
+  const int h = tid >> 9;
+  const int t = tid & 511;
+  const int G = gridDim.x;
+  const int kcount = (ngroups - (int)blockIdx.x + G - 1) / G;  // groups of this CTA
+  if (tid == 0) {
+    for (int b = 0; b < P_BUFS; ++b) mbar_init(sm.bars + b, 1);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int k = 0; k < P_BUFS && k < kcount; ++k)
+      load_group(sm.bufs + (size_t)k * NROWS * SG, sm.bars + k, &tin, blockIdx.x + k * G, gpp);
+  }
+  if (tid < 2) sm.knext[tid] = tid;
+  __syncthreads();
+  const SyncHalf sync{1 + h};
+  for (;;) {
+    const int k = sm.knext[h];
+    if (k >= kcount) break;
+    const int b = k % P_BUFS;
+    double* tile = sm.bufs + (size_t)b * NROWS * SG;
+    if (!sync.all(mbar_wait(sm.bars + b, (unsigned)(k / P_BUFS) & 1u))) {
+      if (t == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
+      return;
+    }
+    const unsigned rmax = strided_group<RHS, SWEEPS>(tile, sm.xch + h * S_XCH_FLOATS, t, a, sync);
+    if (__any_sync(FULL, rmax >= RANGE_MAG) && (t & 31) == 0 && a.status) atomicOr(a.status, 1u);
+    fence_proxy_async();
+    if (t == 0) sm.knext[h] = k + 2;
+    sync();
+    if (t == 0) finish_group(&tin, &tout, gpp, ngroups, h);
   }
 }
 
@@ -507,7 +666,7 @@ int launch_x(const double* in, double* out, const Batch& b, const Args& a, int S
 }
 
 template <int RHS, int SWEEPS>
-int launch_s(const double* in, double* out, const Batch& b, const Args& a, cudaStream_t st) {
+int launch_s(const double* in, double* out, const Batch& b, const Args& a, bool persistent, cudaStream_t st) {
   // dims: system in plane (contiguous), row, plane
   const long long nplanes = b.nsys > b.ni ? b.nsys / b.ni : 1;
   const long long ni = b.nsys > b.ni ? b.ni : b.nsys;
@@ -525,11 +684,23 @@ int launch_s(const double* in, double* out, const Batch& b, const Args& a, cudaS
     set_error("too many systems for one launch");
     return NTK_ERR_INVALID;
   }
-  auto kern = r2s_kernel<RHS, SWEEPS>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_SMEM);
-  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2s_kernel)");
-  kern<<<(unsigned)grid, 32 * CHUNKS / 2, S_SMEM, st>>>(mi, mo, a, (int)gpp);
-  return cuda_status(cudaGetLastError(), "r2s_kernel");
+  if (!persistent) {
+    auto kern = r2s_kernel<RHS, SWEEPS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_SMEM);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2s_kernel)");
+    kern<<<(unsigned)grid, 32 * CHUNKS / 2, S_SMEM, st>>>(mi, mo, a, (int)gpp);
+    return cuda_status(cudaGetLastError(), "r2s_kernel");
+  }
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_status(e, "cudaDeviceGetAttribute(SM count)");
+  auto kern = r2sp_kernel<RHS, SWEEPS>;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P_SMEM);
+  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2sp_kernel)");
+  const long long pgrid = grid < sms ? grid : sms;
+  kern<<<(unsigned)pgrid, 32 * CHUNKS, P_SMEM, st>>>(mi, mo, a, (int)gpp, (int)grid);
+  return cuda_status(cudaGetLastError(), "r2sp_kernel");
 }
 
 }  // namespace
@@ -553,7 +724,7 @@ bool layout_ok(const double* in, const double* out, const Batch& b) {
   return true;
 }
 
-int launch(const double* in, double* out, const Batch& b, const Args& a, int rhs, int sweeps, int S,
+int launch(const double* in, double* out, const Batch& b, const Args& a, int rhs, int sweeps, int S, bool persistent,
            cudaStream_t st) {
   if (S != 4 && S != 8 && S != 16) S = 8;
   if (b.es == 1) {
@@ -561,9 +732,10 @@ int launch(const double* in, double* out, const Batch& b, const Args& a, int rhs
       return sweeps ? launch_x<RHS_COMPACT, 1>(in, out, b, a, S, st) : launch_x<RHS_COMPACT, 0>(in, out, b, a, S, st);
     return sweeps ? launch_x<RHS_IDENTITY, 1>(in, out, b, a, S, st) : launch_x<RHS_IDENTITY, 0>(in, out, b, a, S, st);
   }
+  const bool p = persistent;
   if (rhs == RHS_COMPACT)
-    return sweeps ? launch_s<RHS_COMPACT, 1>(in, out, b, a, st) : launch_s<RHS_COMPACT, 0>(in, out, b, a, st);
-  return sweeps ? launch_s<RHS_IDENTITY, 1>(in, out, b, a, st) : launch_s<RHS_IDENTITY, 0>(in, out, b, a, st);
+    return sweeps ? launch_s<RHS_COMPACT, 1>(in, out, b, a, p, st) : launch_s<RHS_COMPACT, 0>(in, out, b, a, p, st);
+  return sweeps ? launch_s<RHS_IDENTITY, 1>(in, out, b, a, p, st) : launch_s<RHS_IDENTITY, 0>(in, out, b, a, p, st);
 }
 
 }  // namespace r2

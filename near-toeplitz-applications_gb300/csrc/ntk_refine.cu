@@ -216,11 +216,14 @@ int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsPar
     return NTK_ERR_INVALID;
   }
   const int sweeps_eff = (precision == NTK_FP32) ? 0 : sweeps;
-  if (refine->r2_ok && tune_refine_kernel == 0 && sweeps_eff <= 1 && r2::layout_ok(in, out, b)) {
+  if (refine->r2_ok && tune_refine_kernel != 1 && sweeps_eff <= 1 && r2::layout_ok(in, out, b)) {
     r2::Args a2 = refine->r2args;
     r2::set_scales(&a2, rp.sigma0, rp.sigmaN, s);
     a2.status = refine->d_status;
-    return r2::launch(in, out, b, a2, rp.kind, sweeps_eff, tune_refine_w, stream);
+    // strided layouts: persistent CTAs measured faster without refinement,
+    // one group per CTA with it (GB300, 512^3 fields)
+    const bool persistent = tune_refine_kernel == 3 || (tune_refine_kernel == 0 && sweeps_eff == 0);
+    return r2::launch(in, out, b, a2, rp.kind, sweeps_eff, tune_refine_w, persistent, stream);
   }
   RefineArgs ra;
   int M = 0;

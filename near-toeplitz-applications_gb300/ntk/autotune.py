@@ -13,10 +13,11 @@ cached per (device, kernel family, n, precision, layout):
                  threads per system = 32, rows per lane = n / 32 in registers)
   refine_spw     systems per warp (2 stages twice as many adjacent systems
                  per CTA: wider row segments for strided y/z sweeps)
-  refine_kernel  n = 512: 0 the paired-chunk TMA kernels (16 rows per
+  refine_kernel  n = 512: the paired-chunk TMA kernels (16 rows per
                  thread, two 8-row halves per packed FP32x2 instruction;
-                 refine_w = systems per CTA of contiguous layouts), 1 the
-                 chunked kernel (refine_w, refine_spw as above)
+                 refine_w = systems per CTA of contiguous layouts) with one
+                 strided group per CTA (2) or persistent strided CTAs (3);
+                 1 the chunked kernel (refine_w, refine_spw as above)
 
 Usage:
     best = autotune.tune(plan, run, key)   # run() launches the workload once
@@ -32,9 +33,9 @@ _lock = threading.Lock()
 
 SPACE = {
     "fp64": [{"f64_x_variant": [0, 1], "f64_threads": [64, 128]}],
-    "fp32": [{"refine_kernel": [0], "refine_w": [4, 8, 16]},
+    "fp32": [{"refine_kernel": [2, 3], "refine_w": [4, 8, 16]},
              {"refine_kernel": [1], "refine_w": [4, 8, 16], "refine_spw": [1, 2]}],
-    "fp32_refine": [{"refine_kernel": [0], "refine_w": [4, 8, 16]},
+    "fp32_refine": [{"refine_kernel": [2, 3], "refine_w": [4, 8, 16]},
                     {"refine_kernel": [1], "refine_w": [4, 8, 16], "refine_spw": [1, 2]}],
 }
 # a refinement CTA stages at most 16 systems (refine_w * refine_spw)

@@ -19,9 +19,10 @@ def test_candidates_cover_the_space():
     c = autotune.candidates("fp64")
     assert {"f64_x_variant": 0, "f64_threads": 64} in c and len(c) == 4
     c = autotune.candidates("fp32_refine")
-    assert len(c) == 8
+    assert len(c) == 11
     for w in (4, 8, 16):
-        assert {"refine_kernel": 0, "refine_w": w} in c
+        assert {"refine_kernel": 2, "refine_w": w} in c
+        assert {"refine_kernel": 3, "refine_w": w} in c
     assert {"refine_kernel": 1, "refine_w": 8, "refine_spw": 2} in c
     assert {"refine_kernel": 1, "refine_w": 16, "refine_spw": 1} in c
     assert {"refine_kernel": 1, "refine_w": 16, "refine_spw": 2} not in c  # more than 16 systems per CTA
@@ -34,12 +35,12 @@ def test_tune_picks_fastest_and_caches(tmp_path, monkeypatch):
     monkeypatch.setattr(autotune, "device_name", lambda: "FAKE-GPU")
     plan = FakePlan("fp32_refine")
     fake_ms = {(1, 4, 1): 2.0, (1, 8, 1): 1.0, (1, 16, 1): 0.75, (1, 4, 2): 1.5, (1, 8, 2): 0.5,
-               (0, 4, 1): 0.9, (0, 8, 1): 0.6, (0, 16, 1): 0.7}
+               (3, 4, 1): 0.9, (3, 8, 1): 0.6, (3, 16, 1): 0.7, (2, 4, 1): 0.95, (2, 8, 1): 0.65, (2, 16, 1): 0.8}
     best = {"refine_kernel": 1, "refine_w": 8, "refine_spw": 2}
 
     def timer(run, repeats):
         c = plan.cfg
-        return fake_ms[(c["refine_kernel"], c["refine_w"], c.get("refine_spw", 1) if c["refine_kernel"] else 1)]
+        return fake_ms[(c["refine_kernel"], c["refine_w"], c.get("refine_spw", 1) if c["refine_kernel"] == 1 else 1)]
 
     res = autotune.tune(plan, lambda: None, key="compact-x", timer=timer)
     assert res["config"] == best and plan.cfg == best

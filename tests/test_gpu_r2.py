@@ -139,3 +139,24 @@ def test_misaligned_view_falls_back_and_stays_correct(cuda, oracle):
     a, b, c = oracle.near_toeplitz_bands(N, COMPACT)
     ref = np.array([oracle.thomas_ld(a, b, c, row) for row in d])
     assert oracle.rel_err(view.cpu().numpy().reshape(9, N), ref) < 1e-12
+
+
+@pytest.mark.parametrize("shape,axis", [((160, 512, 64), 1), ((512, 96, 112), 0)])
+def test_persistent_ctas_cycle_their_tile_buffers(cuda, r2emu, shape, axis):
+    """Enough 16-system groups (640 and 672) that every persistent CTA (one
+    per SM) reloads each of its three tile buffers at least once; the result
+    equals the emulation bit for bit and the one-group-per-CTA kernel's."""
+    import ntk
+
+    f = _field(shape, seed=5, cuda=cuda)
+    o0, o2 = torch.empty_like(f), torch.empty_like(f)
+    with ntk.Plan(N, 0, COMPACT, precision="fp32_refine") as p:
+        p.set_tuning(refine_kernel=3)
+        p.compact_deriv(f, o0, axis=axis, h=H)
+        p.set_tuning(refine_kernel=2)
+        p.compact_deriv(f, o2, axis=axis, h=H)
+        assert p.status() == 0
+    torch.cuda.synchronize()
+    assert torch.equal(o0, o2)
+    rc, xe = r2emu_solve(r2emu, _lines(f.cpu().numpy(), axis))
+    assert rc == 0 and _bits_equal(_lines(o0.cpu().numpy(), axis), xe)
