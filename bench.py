@@ -468,7 +468,18 @@ def run_gpu(args):
     launch_ms = per_axis[dominant_axis]
     achieved = alg_bytes_launch / (launch_ms * 1e-3) / 1e9
     value = world * ROWS_PER_STEP / (ms_main * 1e-3)
-    traffic = profile_traffic("refine_kernel_512cube" if args.precision != "fp64" else "thomas_f64_512cube")
+    traffic = profile_traffic("r2_kernels_512cube" if args.precision != "fp64" else "thomas_f64_512cube")
+    kind = tuned[(args.precision, dominant_axis)].get("refine_kernel", 0)
+    if args.precision == "fp64":
+        kname = "thomas_f64_kernel"
+    elif kind == 1:
+        kname = "refine_kernel (chunked)"
+    elif dominant_axis == 2:
+        kname = "r2x_kernel"
+    elif kind == 3 or (kind == 0 and args.precision == "fp32"):
+        kname = "r2sp_kernel"
+    else:
+        kname = "r2s_kernel"
     cpu = None
     if not args.no_cpu_baseline:
         rate, rows, wall = cpu_path_rate(4096, 3, 1, reps=40)
@@ -497,8 +508,7 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "%s, axis %s, %d rows x 16 B per launch" % (
-                         "refine_kernel" if args.precision != "fp64" else "thomas_f64_kernel",
-                         "xyz"[2 - dominant_axis], rows_launch)},
+                         kname, "xyz"[2 - dominant_axis], rows_launch)},
         "cpu_baseline": cpu,
         "e2e": {"value": world * ROWS_PER_STEP / (ms_e2e * 1e-3), "unit": "rows/s",
                 "h2d_bytes_per_step": 8 * N ** 3, "d2h_bytes_per_step": 3 * 8 * N ** 3,
