@@ -89,13 +89,17 @@ int ntk_plan_create(ntk_plan** out, int n, long long nrhs, const double coeffs[7
  *                           NTK_FP32_REFINE (faster on GB300); 1 the
  *                           chunked kernel above.  With 0, 2 or 3,
  *                           NTK_TUNE_REFINE_W sets the systems per CTA of
- *                           contiguous layouts (4, 8 or 16). */
+ *                           contiguous layouts (4, 8 or 16).
+ *   NTK_TUNE_REFINE_PREFETCH  the one-group strided kernel: a CTA prefetches
+ *                           into L2 the tile the CTA resident 1 (default)
+ *                           or 2 waves later will load; 0 none. */
 enum ntk_tune_key {
   NTK_TUNE_F64_X_VARIANT = 1,
   NTK_TUNE_F64_THREADS = 2,
   NTK_TUNE_REFINE_W = 3,
   NTK_TUNE_REFINE_SPW = 4,
-  NTK_TUNE_REFINE_KERNEL = 5
+  NTK_TUNE_REFINE_KERNEL = 5,
+  NTK_TUNE_REFINE_PREFETCH = 6
 };
 int ntk_plan_set_tuning(ntk_plan* plan, int key, int value);
 int ntk_plan_get_tuning(const ntk_plan* plan, int key, int* value);

@@ -78,6 +78,7 @@ struct Plan {
   int tune_refine_spw = 1;     // systems per warp (2: strided layouts, 16 rows per lane)
   int tune_refine_kernel = 0;  // n = 512: paired-chunk TMA kernels where they apply (0: automatic, 2: one
                                // strided group per CTA, 3: persistent strided CTAs), 1: the chunked kernel
+  int tune_refine_prefetch = 1;  // one-group strided CTAs: L2 prefetch 0, 1 or 2 waves ahead
 
   int init(int n, long long nrhs, const double co[7], int precision, int sweeps);
   ~Plan();

@@ -72,6 +72,13 @@ __device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, int 
       "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
       : "memory");
 }
+// Fetch a box into L2 only (no shared-memory destination, no completion to
+// wait for): the load that follows finds the box in L2.
+__device__ __forceinline__ void tma_prefetch_l2(const CUtensorMap* map, int c0, int c1, int c2, int c3) {
+  asm volatile("cp.async.bulk.prefetch.tensor.4d.L2.global [%0, {%1, %2, %3, %4}];" ::"l"(map), "r"(c0), "r"(c1),
+               "r"(c2), "r"(c3)
+               : "memory");
+}
 __device__ __forceinline__ void tma_store(const CUtensorMap* map, int c0, int c1, int c2, int c3, const void* src) {
   asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%1, %2, %3, %4}], [%5];" ::"l"(map),
                "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(src))
@@ -471,10 +478,13 @@ __device__ __forceinline__ void group_coords(int g, int gpp, int& x0, int& plane
 }
 
 // One group per CTA.
+// pf_dist > 0: on starting, a CTA prefetches into L2 the tile of the group
+// pf_dist further on, which the CTA resident one wave later loads (pf_dist =
+// the number of CTAs resident at once), so that load is served from L2.
 template <int RHS, int SWEEPS>
 __global__ void __launch_bounds__(512, 2)
     r2s_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
-               const __grid_constant__ Args a, int gpp) {
+               const __grid_constant__ Args a, int gpp, int pf_dist) {
   extern __shared__ unsigned char smem_raw[];
   double* tile = reinterpret_cast<double*>(align1024(smem_raw));  // [512][16]
   float* xch = reinterpret_cast<float*>(tile + NROWS * SG);         // [X_COUNT][32][16]
@@ -488,6 +498,13 @@ __global__ void __launch_bounds__(512, 2)
     mbar_expect_tx(bar, (unsigned)S_TILE_BYTES);
     tma_load(tile, &tin, x0, 0, plane, 0, bar);
     tma_load(tile + (NROWS / 2) * SG, &tin, x0, NROWS / 2, plane, 0, bar);
+    const long long gn = (long long)blockIdx.x + pf_dist;
+    if (pf_dist > 0 && gn < (long long)gridDim.x) {
+      int px, pp;
+      group_coords((int)gn, gpp, px, pp);
+      tma_prefetch_l2(&tin, px, 0, pp, 0);
+      tma_prefetch_l2(&tin, px, NROWS / 2, pp, 0);
+    }
   }
   if (!__syncthreads_and(mbar_wait(bar, 0))) {
     if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
@@ -666,7 +683,8 @@ int launch_x(const double* in, double* out, const Batch& b, const Args& a, int S
 }
 
 template <int RHS, int SWEEPS>
-int launch_s(const double* in, double* out, const Batch& b, const Args& a, bool persistent, cudaStream_t st) {
+int launch_s(const double* in, double* out, const Batch& b, const Args& a, bool persistent, int prefetch,
+             cudaStream_t st) {
   // dims: system in plane (contiguous), row, plane
   const long long nplanes = b.nsys > b.ni ? b.nsys / b.ni : 1;
   const long long ni = b.nsys > b.ni ? b.ni : b.nsys;
@@ -684,17 +702,19 @@ int launch_s(const double* in, double* out, const Batch& b, const Args& a, bool 
     set_error("too many systems for one launch");
     return NTK_ERR_INVALID;
   }
-  if (!persistent) {
-    auto kern = r2s_kernel<RHS, SWEEPS>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_SMEM);
-    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2s_kernel)");
-    kern<<<(unsigned)grid, 32 * CHUNKS / 2, S_SMEM, st>>>(mi, mo, a, (int)gpp);
-    return cuda_status(cudaGetLastError(), "r2s_kernel");
-  }
   int dev = 0, sms = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return cuda_status(e, "cudaDeviceGetAttribute(SM count)");
+  if (!persistent) {
+    auto kern = r2s_kernel<RHS, SWEEPS>;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_SMEM);
+    if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2s_kernel)");
+    // two 512-thread CTAs per SM fill its registers: a wave is 2 * SMs groups
+    const int pf = prefetch * 2 * sms;
+    kern<<<(unsigned)grid, 32 * CHUNKS / 2, S_SMEM, st>>>(mi, mo, a, (int)gpp, pf);
+    return cuda_status(cudaGetLastError(), "r2s_kernel");
+  }
   auto kern = r2sp_kernel<RHS, SWEEPS>;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P_SMEM);
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2sp_kernel)");
@@ -725,7 +745,7 @@ bool layout_ok(const double* in, const double* out, const Batch& b) {
 }
 
 int launch(const double* in, double* out, const Batch& b, const Args& a, int rhs, int sweeps, int S, bool persistent,
-           cudaStream_t st) {
+           int prefetch, cudaStream_t st) {
   if (S != 4 && S != 8 && S != 16) S = 8;
   if (b.es == 1) {
     if (rhs == RHS_COMPACT)
@@ -733,9 +753,11 @@ int launch(const double* in, double* out, const Batch& b, const Args& a, int rhs
     return sweeps ? launch_x<RHS_IDENTITY, 1>(in, out, b, a, S, st) : launch_x<RHS_IDENTITY, 0>(in, out, b, a, S, st);
   }
   const bool p = persistent;
+  const int f = prefetch;
   if (rhs == RHS_COMPACT)
-    return sweeps ? launch_s<RHS_COMPACT, 1>(in, out, b, a, p, st) : launch_s<RHS_COMPACT, 0>(in, out, b, a, p, st);
-  return sweeps ? launch_s<RHS_IDENTITY, 1>(in, out, b, a, p, st) : launch_s<RHS_IDENTITY, 0>(in, out, b, a, p, st);
+    return sweeps ? launch_s<RHS_COMPACT, 1>(in, out, b, a, p, f, st) : launch_s<RHS_COMPACT, 0>(in, out, b, a, p, f, st);
+  return sweeps ? launch_s<RHS_IDENTITY, 1>(in, out, b, a, p, f, st)
+                : launch_s<RHS_IDENTITY, 0>(in, out, b, a, p, f, st);
 }
 
 }  // namespace r2

@@ -12,9 +12,10 @@ bool layout_ok(const double* in, const double* out, const Batch& b);
 // The solve (rhs: RHS_IDENTITY or RHS_COMPACT; sweeps 0 or 1), S systems
 // per CTA for contiguous systems (4, 8 or 16); strided systems run
 // persistent CTAs (one per SM, a tile loading while two are solved) or one
-// group per CTA.
+// group per CTA; prefetch (0, 1, 2): how many waves ahead a one-group CTA
+// prefetches a tile into L2.
 int launch(const double* in, double* out, const Batch& b, const Args& a, int rhs, int sweeps, int S, bool persistent,
-           cudaStream_t st);
+           int prefetch, cudaStream_t st);
 
 }  // namespace r2
 }  // namespace ntk

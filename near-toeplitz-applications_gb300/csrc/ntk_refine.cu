@@ -223,7 +223,7 @@ int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsPar
     // strided layouts: persistent CTAs measured faster without refinement,
     // one group per CTA with it (GB300, 512^3 fields)
     const bool persistent = tune_refine_kernel == 3 || (tune_refine_kernel == 0 && sweeps_eff == 0);
-    return r2::launch(in, out, b, a2, rp.kind, sweeps_eff, tune_refine_w, persistent, stream);
+    return r2::launch(in, out, b, a2, rp.kind, sweeps_eff, tune_refine_w, persistent, tune_refine_prefetch, stream);
   }
   RefineArgs ra;
   int M = 0;

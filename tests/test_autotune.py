@@ -19,9 +19,9 @@ def test_candidates_cover_the_space():
     c = autotune.candidates("fp64")
     assert {"f64_x_variant": 0, "f64_threads": 64} in c and len(c) == 4
     c = autotune.candidates("fp32_refine")
-    assert len(c) == 11
+    assert len(c) == 17
     for w in (4, 8, 16):
-        assert {"refine_kernel": 2, "refine_w": w} in c
+        assert {"refine_kernel": 2, "refine_w": w, "refine_prefetch": 1} in c
         assert {"refine_kernel": 3, "refine_w": w} in c
     assert {"refine_kernel": 1, "refine_w": 8, "refine_spw": 2} in c
     assert {"refine_kernel": 1, "refine_w": 16, "refine_spw": 1} in c
@@ -40,13 +40,14 @@ def test_tune_picks_fastest_and_caches(tmp_path, monkeypatch):
 
     def timer(run, repeats):
         c = plan.cfg
-        return fake_ms[(c["refine_kernel"], c["refine_w"], c.get("refine_spw", 1) if c["refine_kernel"] == 1 else 1)]
+        return fake_ms[(c["refine_kernel"], c["refine_w"], c.get("refine_spw", 1) if c["refine_kernel"] == 1 else 1)] \
+            + 0.01 * c.get("refine_prefetch", 0)
 
     res = autotune.tune(plan, lambda: None, key="compact-x", timer=timer)
-    assert res["config"] == best and plan.cfg == best
+    assert res["config"] == best and all(plan.cfg[k] == v for k, v in best.items())
     plan2 = FakePlan("fp32_refine")
     assert autotune.apply_cached(plan2, "compact-x") == best
-    assert plan2.cfg == best
+    assert all(plan2.cfg[k] == v for k, v in best.items())
     # a cache hit does not time again
     res2 = autotune.tune(FakePlan("fp32_refine"), lambda: None, key="compact-x",
                          timer=lambda *a: pytest.fail("timed despite cache"))
