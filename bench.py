@@ -393,6 +393,23 @@ def run_gpu(args):
     _, per_axis = timed(main, max(2, args.steps // 2), 1, per_launch=True)
     ms_fp64, per_axis64 = timed(plans["fp64"], max(2, args.steps // 2), 1, per_launch=True)
     ms_fp32, _ = timed(plans["fp32"], max(2, args.steps // 2), 1)
+
+    # the same step as one call of ntk_compact_grad: one launch of the
+    # combined kernel (x and y groups of each z-plane side by side, then z)
+    def timed_grad(plan, steps, warmup):
+        for _ in range(warmup):
+            plan.compact_grad(f, outs[0], outs[1], outs[2], h=h)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            plan.compact_grad(f, outs[0], outs[1], outs[2], h=h)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / steps
+
+    ms_grad = timed_grad(main, max(2, args.steps // 2), 2)
     ms_main = max_over_ranks(ms_main, world, dev)
     ms_fp64 = max_over_ranks(ms_fp64, world, dev)
 
@@ -502,6 +519,9 @@ def run_gpu(args):
                  "hbm_frac": (BYTES_PER_ROW * N ** 3 / (per_axis64[max(per_axis64, key=per_axis64.get)] * 1e-3) / 1e9)
                  / hbm},
         "fp32_only": {"ms_per_step": ms_fp32, "rows_per_s": world * ROWS_PER_STEP / (ms_fp32 * 1e-3)},
+        "one_launch": {"ms_per_step": ms_grad, "rows_per_s": world * ROWS_PER_STEP / (ms_grad * 1e-3),
+                       "hbm_frac_48B": 48.0 * N ** 3 / (ms_grad * 1e-3) / 1e9 / hbm,
+                       "call": "ntk_compact_grad: dfdx, dfdy, dfdz in one kernel launch"},
         "speedup_vs_fp64": ms_fp64 / ms_main,
         "errors": errs,
         "per_axis_ms": {"x": per_axis.get(2), "y": per_axis.get(1), "z": per_axis.get(0)},

@@ -145,6 +145,16 @@ int ntk_solve_strided(ntk_plan* plan, const double* d_in, double* d_out, long lo
 int ntk_compact_deriv(ntk_plan* plan, const double* f, double* out, int nz, int ny, int nx, int axis, double h,
                       void* stream);
 
+/* The three compact derivatives of an n x n x n field (nz = ny = nx = the
+ * plan's n) into three separate arrays: the whole of
+ * experiments/run-compact.py:47-90 in one call.  For n = 512 on the
+ * NTK_FP32 / NTK_FP32_REFINE paths of the paired-chunk solve this is ONE
+ * kernel launch: per z-plane its x and y groups run side by side (the plane
+ * is read from HBM once for both), then the z groups; otherwise it is three
+ * ntk_compact_deriv calls.  f and the outputs must not overlap. */
+int ntk_compact_grad(ntk_plan* plan, const double* f, double* dfdx, double* dfdy, double* dfdz, int nz, int ny,
+                     int nx, double h, void* stream);
+
 /* compute_rhs(f, rhs, dx) of compact/rhs.py:47-53: the RHS along the last
  * axis of an [nz][ny][nx] field.  Any nz, ny >= 1 and nx >= 3 (the
  * reference needs multiples of 8). */
@@ -209,6 +219,26 @@ int ntk_adi_step(ntk_adi* adi, double* u, double* d_x, const double* d_y, void* 
 /* `steps` time steps.  use_graph != 0 captures the steps once per
  * (u, d_x, d_y, steps) into a CUDA graph and replays it on later calls. */
 int ntk_adi_run(ntk_adi* adi, double* u, double* d_x, const double* d_y, int steps, int use_graph, void* stream);
+
+/* ---- ADI with per-line coefficients ----------------------------------------
+ * Generalises the reference's single ADI matrix (run-adi.py:50-53, the
+ * model of neato.py:136-138) to one near-Toeplitz system per line:
+ * u_t = kx(y) u_xx + ky(x) u_yy, kx[j] the x diffusivity on row j, ky[i] the
+ * y diffusivity on column i (kx = ky = 1 is the reference's step).  A step
+ * follows run-adi.py:59-71: the stencil of adi/rhs.py:21-24 with per-column
+ * coefficients (-k/dx^2, 2(-1/dt + k/dx^2), -k/dx^2) into d_x, the rows
+ * 1..N-2 of d_x solved with (1, 0 | a, -2(1/dt + a), a | 0, 1), a = k/dx^2 of
+ * their own line (uneven batches: FP64 windows, or FP32 + refinement
+ * windows with NTK_FP32_REFINE), u = d_x^T, and the same into d_y, u = d_y^T.
+ * d_x and d_y keep their boundary values (the reference initialises d_x = u,
+ * d_y = u^T).  Create and destroy are synchronous. */
+typedef struct ntk_adi_var ntk_adi_var;
+int ntk_adi_var_create(ntk_adi_var** out, int N, double dx, double dt, const double* kx, const double* ky,
+                       int precision);
+int ntk_adi_var_destroy(ntk_adi_var* adi);
+int ntk_adi_var_step(ntk_adi_var* adi, double* u, double* d_x, double* d_y, void* stream);
+/* ntk_plan_status for the per-line batches' FP32 windows.  Synchronous. */
+int ntk_adi_var_status(ntk_adi_var* adi, int* flags, void* stream);
 
 /* ---- ADI step that allocates nothing ----------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

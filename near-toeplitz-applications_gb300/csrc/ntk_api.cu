@@ -389,6 +389,35 @@ int ntk_compact_deriv(ntk_plan* plan, const double* f, double* out, int nz, int 
   return plan->run(f, out, b, rp, s, (cudaStream_t)stream);
 }
 
+int ntk_compact_grad(ntk_plan* plan, const double* f, double* dfdx, double* dfdy, double* dfdz, int nz, int ny,
+                     int nx, double h, void* stream) {
+  if (!plan || ntk::bad_ptr(f) || ntk::bad_ptr(dfdx) || ntk::bad_ptr(dfdy) || ntk::bad_ptr(dfdz)) {
+    ntk::set_error("ntk_compact_grad: null plan or null/misaligned pointer");
+    return NTK_ERR_INVALID;
+  }
+  if (nz != plan->n || ny != plan->n || nx != plan->n || !(h > 0) || !std::isfinite(h)) {
+    ntk::set_error("ntk_compact_grad: the field must be n x n x n with the plan's n = %d, h > 0", plan->n);
+    return NTK_ERR_INVALID;
+  }
+  const long long total = (long long)nz * ny * nx;
+  const double* arr[4] = {f, dfdx, dfdy, dfdz};
+  for (int i = 0; i < 4; ++i)
+    for (int k = i + 1; k < 4; ++k)
+      if (arr[i] < arr[k] + total && arr[k] < arr[i] + total) {
+        ntk::set_error("ntk_compact_grad: f and the three outputs must not overlap");
+        return NTK_ERR_INVALID;
+      }
+  const cudaStream_t st = (cudaStream_t)stream;
+  if (plan->precision != NTK_FP64) {
+    const int rc = plan->run_grad(f, dfdx, dfdy, dfdz, h, st);
+    if (rc != NTK_ERR_UNSUPPORTED) return rc;
+  }
+  int rc = ntk_compact_deriv(plan, f, dfdx, nz, ny, nx, 2, h, stream);
+  if (!rc) rc = ntk_compact_deriv(plan, f, dfdy, nz, ny, nx, 1, h, stream);
+  if (!rc) rc = ntk_compact_deriv(plan, f, dfdz, nz, ny, nx, 0, h, stream);
+  return rc;
+}
+
 int ntk_compact_rhs(const double* f, double* rhs, int nz, int ny, int nx, double dx, void* stream) {
   if (ntk::bad_ptr(f) || ntk::bad_ptr(rhs)) {
     ntk::set_error("ntk_compact_rhs: null/misaligned pointer");

@@ -90,6 +90,9 @@ struct Plan {
   int init_refine();
   int run_refine(const double* in, double* out, const Batch& b, const RhsParams& rp, double s, cudaStream_t stream);
   void release_refine();
+  // the three derivatives of an n^3 field in one launch (ntk_r2.cu);
+  // NTK_ERR_UNSUPPORTED where that kernel does not apply
+  int run_grad(const double* f, double* ox, double* oy, double* oz, double h, cudaStream_t stream);
   // device status words of this plan's FP32 kernels (none for NTK_FP64)
   void status_words(std::vector<unsigned*>& out) const;
 };

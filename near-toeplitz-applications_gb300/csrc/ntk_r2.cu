@@ -94,6 +94,29 @@ __device__ __forceinline__ unsigned char* align1024(unsigned char* p) {
   return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~(uintptr_t)1023);
 }
 
+// Barriers over the threads that work on one group: the whole CTA, or a
+// named barrier (id 1..15) over `count` threads of it.  all(v): a barrier
+// that also returns whether v holds in every participating thread.
+struct SyncAll {
+  __device__ __forceinline__ void operator()() const { __syncthreads(); }
+  __device__ __forceinline__ bool all(bool v) const { return __syncthreads_and(v) != 0; }
+};
+struct SyncBar {
+  int id, count;
+  __device__ __forceinline__ void operator()() const {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+  }
+  __device__ __forceinline__ bool all(bool v) const {
+    unsigned r;
+    asm volatile(
+        "{ .reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.and.pred q, %2, %3, p; selp.u32 %0, 1, 0, q; }"
+        : "=r"(r)
+        : "r"((unsigned)v), "r"(id), "r"(count)
+        : "memory");
+    return r != 0;
+  }
+};
+
 // ---------------------------------------------------------------------------
 // contiguous systems
 // ---------------------------------------------------------------------------
@@ -101,27 +124,23 @@ __device__ __forceinline__ unsigned char* align1024(unsigned char* p) {
 // written by TMA with the 128-byte swizzle: 16-byte unit i XOR (j mod 8).
 __device__ __forceinline__ int xpair(int j, int i) { return j * 16 + ((i ^ (j & 7)) << 1); }
 
-template <int RHS, int SWEEPS>
-__global__ void __launch_bounds__(512, 2)
-    r2x_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
-               const __grid_constant__ Args a, int gpp) {
-  extern __shared__ unsigned char smem_raw[];
-  double* tile = reinterpret_cast<double*>(align1024(smem_raw));
-  const int S = blockDim.x >> 5;
-  float2* bnd = reinterpret_cast<float2*>(tile + S * NROWS);  // [S][2]: rows 0 and n-1
-  uint64_t* bar = reinterpret_cast<uint64_t*>(bnd + 2 * S);
-  const int tid = threadIdx.x, warp = tid >> 5, j = tid & 31;
-  const int plane = blockIdx.x / gpp;
-  const int s0 = (blockIdx.x - plane * gpp) * S;
-  if (tid == 0) mbar_init(bar, 1);
-  __syncthreads();
-  if (tid == 0) {
+// S contiguous systems (one warp each) solved in place in their swizzled
+// tile by the S * 32 threads gt = 0 .. of a group: TMA load of the box at
+// coordinates (0, 0, c2, c3) of tin, solve, TMA store to tout.
+template <int RHS, int SWEEPS, class SYNC>
+__device__ __forceinline__ void contiguous_group(double* tile, float2* bnd, uint64_t* bar, const CUtensorMap* tin,
+                                                 const CUtensorMap* tout, int S, int gt, int c2, int c3,
+                                                 const Args& a, SYNC sync) {
+  const int warp = gt >> 5, j = gt & 31;
+  if (gt == 0) mbar_init(bar, 1);
+  sync();
+  if (gt == 0) {
     mbar_expect_tx(bar, (unsigned)S * NROWS * 8u);
-    tma_load(tile, &tin, 0, 0, s0, plane, bar);
+    tma_load(tile, tin, 0, 0, c2, c3, bar);
   }
-  // every thread waits (bounded); the CTA gives up together if any did
-  if (!__syncthreads_and(mbar_wait(bar, 0))) {
-    if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
+  // every thread waits (bounded); the group gives up together if any did
+  if (!sync.all(mbar_wait(bar, 0))) {
+    if (gt == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
     return;
   }
   const Consts& K = a.k;
@@ -139,7 +158,7 @@ __global__ void __launch_bounds__(512, 2)
       boundary_rhs(r0, r1, r2, tl ? a.sigmaN : a.sigma0, h, l, rmax);
       bnd[j] = make_float2(h, l);
     }
-    __syncthreads();
+    sync();
   }
   double* sy = tile + warp * NROWS;
   float2 v[8];
@@ -286,11 +305,26 @@ __global__ void __launch_bounds__(512, 2)
   }
   if (__any_sync(FULL, rmax >= RANGE_MAG) && j == 0 && a.status) atomicOr(a.status, 1u);
   fence_proxy_async();
-  __syncthreads();
-  if (tid == 0) {
-    tma_store(&tout, 0, 0, s0, plane, tile);
+  sync();
+  if (gt == 0) {
+    tma_store(tout, 0, 0, c2, c3, tile);
     tma_store_commit_and_wait();
   }
+}
+
+// One group of S = blockDim.x / 32 contiguous systems per CTA.
+template <int RHS, int SWEEPS>
+__global__ void __launch_bounds__(512, 2)
+    r2x_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
+               const __grid_constant__ Args a, int gpp) {
+  extern __shared__ unsigned char smem_raw[];
+  double* tile = reinterpret_cast<double*>(align1024(smem_raw));
+  const int S = blockDim.x >> 5;
+  float2* bnd = reinterpret_cast<float2*>(tile + S * NROWS);  // [S][2]: rows 0 and n-1
+  uint64_t* bar = reinterpret_cast<uint64_t*>(bnd + 2 * S);
+  const int plane = blockIdx.x / gpp;
+  const int s0 = (blockIdx.x - plane * gpp) * S;
+  contiguous_group<RHS, SWEEPS>(tile, bnd, bar, &tin, &tout, S, threadIdx.x, s0, plane, a, SyncAll());
 }
 
 // ---------------------------------------------------------------------------
@@ -305,26 +339,6 @@ constexpr size_t S_SMEM = 1024 + S_TILE_BYTES + S_XCH_FLOATS * 4 + 16;
 // the persistent kernel: two groups in compute, a third tile loading
 constexpr int P_BUFS = 3;
 constexpr size_t P_SMEM = 1024 + P_BUFS * S_TILE_BYTES + 2 * S_XCH_FLOATS * 4 + 8 * P_BUFS + 8;
-
-// CTA barrier of the 512 threads that work on one group: all of a
-// one-group CTA, or one half of a persistent CTA (named barrier 1 or 2).
-struct SyncAll {
-  __device__ __forceinline__ void operator()() const { __syncthreads(); }
-};
-struct SyncHalf {
-  int id;
-  __device__ __forceinline__ void operator()() const { asm volatile("bar.sync %0, 512;" ::"r"(id) : "memory"); }
-  // barrier that also returns whether v holds in all 512 threads
-  __device__ __forceinline__ bool all(bool v) const {
-    unsigned r;
-    asm volatile(
-        "{ .reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.and.pred q, %2, 512, p; selp.u32 %0, 1, 0, q; }"
-        : "=r"(r)
-        : "r"((unsigned)v), "r"(id)
-        : "memory");
-    return r != 0;
-  }
-};
 
 // One group of 16 systems, solved in place in its [512][16] tile by 512
 // threads: thread t owns system t % 16 and chunk t / 16.  The first and
@@ -478,6 +492,36 @@ __device__ __forceinline__ void group_coords(int g, int gpp, int& x0, int& plane
 }
 
 // One group per CTA.
+// One 16-system strided group per CTA, boxes at (x0, 0 | 256, plane, 0):
+// load, solve, store.  prefetch() runs on thread 0 once its own load is
+// issued.
+template <int RHS, int SWEEPS, class PF>
+__device__ __forceinline__ void strided_cta(double* tile, float* xch, uint64_t* bar, const CUtensorMap* tin,
+                                            const CUtensorMap* tout, int x0, int plane, const Args& a, PF prefetch) {
+  const int tid = threadIdx.x;
+  if (tid == 0) mbar_init(bar, 1);
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(bar, (unsigned)S_TILE_BYTES);
+    tma_load(tile, tin, x0, 0, plane, 0, bar);
+    tma_load(tile + (NROWS / 2) * SG, tin, x0, NROWS / 2, plane, 0, bar);
+    prefetch();
+  }
+  if (!__syncthreads_and(mbar_wait(bar, 0))) {
+    if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
+    return;
+  }
+  const unsigned rmax = strided_group<RHS, SWEEPS>(tile, xch, tid, a, SyncAll());
+  if (__any_sync(FULL, rmax >= RANGE_MAG) && (tid & 31) == 0 && a.status) atomicOr(a.status, 1u);
+  fence_proxy_async();
+  __syncthreads();
+  if (tid == 0) {
+    tma_store(tout, x0, 0, plane, 0, tile);
+    tma_store(tout, x0, NROWS / 2, plane, 0, tile + (NROWS / 2) * SG);
+    tma_store_commit_and_wait();
+  }
+}
+
 // pf_dist > 0: on starting, a CTA prefetches into L2 the tile of the group
 // pf_dist further on, which the CTA resident one wave later loads (pf_dist =
 // the number of CTAs resident at once), so that load is served from L2.
@@ -489,15 +533,9 @@ __global__ void __launch_bounds__(512, 2)
   double* tile = reinterpret_cast<double*>(align1024(smem_raw));  // [512][16]
   float* xch = reinterpret_cast<float*>(tile + NROWS * SG);         // [X_COUNT][32][16]
   uint64_t* bar = reinterpret_cast<uint64_t*>(xch + S_XCH_FLOATS);
-  const int tid = threadIdx.x;
   int x0, plane;
   group_coords(blockIdx.x, gpp, x0, plane);
-  if (tid == 0) mbar_init(bar, 1);
-  __syncthreads();
-  if (tid == 0) {
-    mbar_expect_tx(bar, (unsigned)S_TILE_BYTES);
-    tma_load(tile, &tin, x0, 0, plane, 0, bar);
-    tma_load(tile + (NROWS / 2) * SG, &tin, x0, NROWS / 2, plane, 0, bar);
+  strided_cta<RHS, SWEEPS>(tile, xch, bar, &tin, &tout, x0, plane, a, [&] {
     const long long gn = (long long)blockIdx.x + pf_dist;
     if (pf_dist > 0 && gn < (long long)gridDim.x) {
       int px, pp;
@@ -505,19 +543,82 @@ __global__ void __launch_bounds__(512, 2)
       tma_prefetch_l2(&tin, px, 0, pp, 0);
       tma_prefetch_l2(&tin, px, NROWS / 2, pp, 0);
     }
+  });
+}
+
+// ---------------------------------------------------------------------------
+// the three directional derivatives of an n^3 field in one launch
+// ---------------------------------------------------------------------------
+// CTA b: for each z-plane p, the plane's x CTAs (cx of them, 16 x-lines each
+// as four independent 4-system groups) and then its y CTAs (cy, 16 columns
+// each) -- consecutive CTAs, so a plane read from HBM by one axis is in L2
+// for the other -- and after all planes the z CTAs (gz, 16 columns each).
+struct GradGeom {
+  int nz, cx, cy, gz;
+  int pf;  // prefetch distance in CTAs (0: none)
+};
+constexpr int GX_SUB = 4;  // systems per x sub-group (one 128-thread group)
+constexpr size_t G_SMEM = S_SMEM > 1024 + (size_t)4 * GX_SUB * NROWS * 8 + 4 * GX_SUB * 16 + 4 * 8 + 16
+                              ? S_SMEM
+                              : 1024 + (size_t)4 * GX_SUB * NROWS * 8 + 4 * GX_SUB * 16 + 4 * 8 + 16;
+
+__device__ __forceinline__ void grad_prefetch(const CUtensorMap* mx, const CUtensorMap* my, const CUtensorMap* mz,
+                                              const GradGeom& g, long long b) {
+  const long long nxy = (long long)g.nz * (g.cx + g.cy);
+  if (b < nxy) {
+    const int p = (int)(b / (g.cx + g.cy)), r = (int)(b % (g.cx + g.cy));
+    if (r < g.cx) {
+      for (int q = 0; q < 4; ++q) tma_prefetch_l2(mx, 0, 0, r * 16 + q * GX_SUB, p);
+    } else {
+      tma_prefetch_l2(my, (r - g.cx) * SG, 0, p, 0);
+      tma_prefetch_l2(my, (r - g.cx) * SG, NROWS / 2, p, 0);
+    }
+  } else if (b - nxy < g.gz) {
+    const int c0 = (int)(b - nxy) * SG;
+    tma_prefetch_l2(mz, c0, 0, 0, 0);
+    tma_prefetch_l2(mz, c0, NROWS / 2, 0, 0);
   }
-  if (!__syncthreads_and(mbar_wait(bar, 0))) {
-    if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
-    return;
-  }
-  const unsigned rmax = strided_group<RHS, SWEEPS>(tile, xch, tid, a, SyncAll());
-  if (__any_sync(FULL, rmax >= RANGE_MAG) && (tid & 31) == 0 && a.status) atomicOr(a.status, 1u);
-  fence_proxy_async();
-  __syncthreads();
-  if (tid == 0) {
-    tma_store(&tout, x0, 0, plane, 0, tile);
-    tma_store(&tout, x0, NROWS / 2, plane, 0, tile + (NROWS / 2) * SG);
-    tma_store_commit_and_wait();
+}
+
+template <int SWEEPS>
+__global__ void __launch_bounds__(512, 2)
+    r2g_kernel(const __grid_constant__ CUtensorMap fx, const __grid_constant__ CUtensorMap ox,
+               const __grid_constant__ CUtensorMap fy, const __grid_constant__ CUtensorMap oy,
+               const __grid_constant__ CUtensorMap fz, const __grid_constant__ CUtensorMap oz,
+               const __grid_constant__ Args ax, const __grid_constant__ GradGeom g) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base = align1024(smem_raw);
+  const long long b = blockIdx.x;
+  const long long nxy = (long long)g.nz * (g.cx + g.cy);
+  auto prefetch = [&] {
+    if (g.pf > 0) grad_prefetch(&fx, &fy, &fz, g, b + g.pf);
+  };
+  if (b < nxy) {
+    const int p = (int)(b / (g.cx + g.cy)), r = (int)(b % (g.cx + g.cy));
+    if (r < g.cx) {
+      // x: four independent 4-warp groups, each with its own tile, barrier
+      // and named CTA barrier
+      const int q = threadIdx.x >> 7;
+      double* tiles = reinterpret_cast<double*>(base);                     // [4][GX_SUB][512]
+      float2* bnds = reinterpret_cast<float2*>(tiles + 4 * GX_SUB * NROWS);  // [4][2 GX_SUB]
+      uint64_t* bars = reinterpret_cast<uint64_t*>(bnds + 4 * 2 * GX_SUB);   // [4]
+      double* tile = tiles + (size_t)q * GX_SUB * NROWS;
+      float2* bnd = bnds + q * 2 * GX_SUB;
+      uint64_t* bar = bars + q;
+      if (threadIdx.x == 0) prefetch();
+      contiguous_group<RHS_COMPACT, SWEEPS>(tile, bnd, bar, &fx, &ox, GX_SUB, threadIdx.x & 127, r * 16 + q * GX_SUB,
+                                            p, ax, SyncBar{1 + q, 128});
+    } else {
+      double* tile = reinterpret_cast<double*>(base);
+      float* xch = reinterpret_cast<float*>(tile + NROWS * SG);
+      uint64_t* bar = reinterpret_cast<uint64_t*>(xch + S_XCH_FLOATS);
+      strided_cta<RHS_COMPACT, SWEEPS>(tile, xch, bar, &fy, &oy, (r - g.cx) * SG, p, ax, prefetch);
+    }
+  } else {
+    double* tile = reinterpret_cast<double*>(base);
+    float* xch = reinterpret_cast<float*>(tile + NROWS * SG);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(xch + S_XCH_FLOATS);
+    strided_cta<RHS_COMPACT, SWEEPS>(tile, xch, bar, &fz, &oz, (int)(b - nxy) * SG, 0, ax, prefetch);
   }
 }
 
@@ -593,7 +694,7 @@ __global__ void __launch_bounds__(1024, 1)
   }
   if (tid < 2) sm.knext[tid] = tid;
   __syncthreads();
-  const SyncHalf sync{1 + h};
+  const SyncBar sync{1 + h, 512};
   for (;;) {
     const int k = sm.knext[h];
     if (k >= kcount) break;
@@ -742,6 +843,49 @@ bool layout_ok(const double* in, const double* out, const Batch& b) {
   if (b.is != 1 || (b.es & 1) || b.es < ni) return false;
   if (nplanes > 1 && ((b.os & 1) || b.os < b.es * NROWS)) return false;
   return true;
+}
+
+int launch_grad(const double* f, double* ox, double* oy, double* oz, const Args& a, int sweeps, int prefetch,
+                cudaStream_t st) {
+  const cuuint64_t n = NROWS;
+  if (!aligned16(f) || !aligned16(ox) || !aligned16(oy) || !aligned16(oz)) {
+    set_error("one-launch gradient needs 16-byte aligned arrays");
+    return NTK_ERR_UNSUPPORTED;
+  }
+  // x: row in chunk, chunk, line (y), plane (z); box = one 4-system group
+  const cuuint64_t dx[4] = {16, 32, n, n};
+  const cuuint64_t sx[3] = {128, n * 8, n * n * 8};
+  const cuuint32_t bx[4] = {16, 32, (cuuint32_t)GX_SUB, 1};
+  // y: x (contiguous), y rows, z planes; z: (x, y) flattened, z rows
+  const cuuint64_t dy[4] = {n, n, n, 1};
+  const cuuint64_t sy[3] = {n * 8, n * n * 8, n * n * n * 8};
+  const cuuint64_t dz[4] = {n * n, n, 1, 1};
+  const cuuint64_t sz[3] = {n * n * 8, n * n * n * 8, n * n * n * 8};
+  const cuuint32_t bs[4] = {(cuuint32_t)SG, (cuuint32_t)(NROWS / 2), 1, 1};
+  CUtensorMap m[6];
+  int rc = encode(&m[0], f, dx, sx, bx, CU_TENSOR_MAP_SWIZZLE_128B);
+  if (!rc) rc = encode(&m[1], ox, dx, sx, bx, CU_TENSOR_MAP_SWIZZLE_128B);
+  if (!rc) rc = encode(&m[2], f, dy, sy, bs, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if (!rc) rc = encode(&m[3], oy, dy, sy, bs, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if (!rc) rc = encode(&m[4], f, dz, sz, bs, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if (!rc) rc = encode(&m[5], oz, dz, sz, bs, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if (rc) return rc;
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return cuda_status(e, "cudaDeviceGetAttribute(SM count)");
+  GradGeom g;
+  g.nz = NROWS;
+  g.cx = NROWS / 16;
+  g.cy = NROWS / SG;
+  g.gz = NROWS * NROWS / SG;
+  g.pf = prefetch * 2 * sms;
+  const long long grid = (long long)g.nz * (g.cx + g.cy) + g.gz;
+  auto kern = sweeps ? r2g_kernel<1> : r2g_kernel<0>;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM);
+  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2g_kernel)");
+  kern<<<(unsigned)grid, 512, G_SMEM, st>>>(m[0], m[1], m[2], m[3], m[4], m[5], a, g);
+  return cuda_status(cudaGetLastError(), "r2g_kernel");
 }
 
 int launch(const double* in, double* out, const Batch& b, const Args& a, int rhs, int sweeps, int S, bool persistent,

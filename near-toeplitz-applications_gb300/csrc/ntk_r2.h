@@ -17,5 +17,11 @@ bool layout_ok(const double* in, const double* out, const Batch& b);
 int launch(const double* in, double* out, const Batch& b, const Args& a, int rhs, int sweeps, int S, bool persistent,
            int prefetch, cudaStream_t st);
 
+// dfdx, dfdy, dfdz of a 512^3 field f (compact RHS, a's scales set) in one
+// launch: per z-plane the x and y groups next to each other (the plane is
+// read from HBM once for both), then the z groups.
+int launch_grad(const double* f, double* ox, double* oy, double* oz, const Args& a, int sweeps, int prefetch,
+                cudaStream_t st);
+
 }  // namespace r2
 }  // namespace ntk

@@ -248,6 +248,20 @@ int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsPar
   }
 }
 
+int Plan::run_grad(const double* f, double* ox, double* oy, double* oz, double h, cudaStream_t stream) {
+  const int sweeps_eff = (precision == NTK_FP32) ? 0 : sweeps;
+  if (!refine || !refine->r2_ok || n != r2::NROWS || sweeps_eff > 1 || tune_refine_kernel == 1) {
+    set_error("the one-launch gradient serves n = 512 FP32 / FP32+refine plans of the paired-chunk solve");
+    return NTK_ERR_UNSUPPORTED;
+  }
+  r2::Args a2 = refine->r2args;
+  // compact/rhs.py:21-36: interior scale 3/(4h), boundary rows +-1/(2h)
+  const double s = 3. / (4 * h);
+  r2::set_scales(&a2, (1. / (2 * h)) / s, -(1. / (2 * h)) / s, s);
+  a2.status = refine->d_status;
+  return r2::launch_grad(f, ox, oy, oz, a2, sweeps_eff, tune_refine_prefetch, stream);
+}
+
 int refine_args(const Plan& p, double sigma0, double sigmaN, double s, RefineArgs* out, int* Mout, bool* pow2,
                 bool* decay) {
   const RefineState* st = p.refine;

@@ -19,7 +19,7 @@ import ctypes
 from . import _lib
 from ._lib import NtkError, PRECISIONS, check, load  # noqa: F401
 
-__all__ = ["Plan", "Adi", "UnevenBatch", "compact_rhs", "permute3d", "adi_rhs", "transpose2d", "NtkError", "device_ptr",
+__all__ = ["Plan", "Adi", "AdiVar", "UnevenBatch", "compact_rhs", "permute3d", "adi_rhs", "transpose2d", "NtkError", "device_ptr",
            "current_stream", "version"]
 
 COMPACT_COEFFS = (1., 2., 1. / 4, 1., 1. / 4, 2., 1.)  # experiments/run-compact.py:48
@@ -202,6 +202,17 @@ class Plan:
                                        float(h), _stream(stream, f)))
 
 
+    def compact_grad(self, f, dfdx, dfdy, dfdz, h, stream=None):
+        """dfdx, dfdy, dfdz of the n x n x n field f (experiments/run-compact.py:47-90
+        in one call; one kernel launch for n = 512 on the FP32 paths)."""
+        for t in (f, dfdx, dfdy, dfdz):
+            if _is_torch(t) and not t.is_contiguous():
+                raise ValueError("ntk: arrays must be C-contiguous")
+        nz, ny, nx = [int(v) for v in f.shape]
+        check(load().ntk_compact_grad(self.handle, device_ptr(f), device_ptr(dfdx), device_ptr(dfdy),
+                                      device_ptr(dfdz), nz, ny, nx, float(h), _stream(stream, f)))
+
+
 class Adi:
     """Peaceman-Rachford ADI stepper for N x N fields (experiments/run-adi.py).
 
@@ -247,6 +258,60 @@ class Adi:
         if getattr(self, "_h", None) is not None:
             try:
                 load().ntk_adi_destroy(self._h)
+            finally:
+                self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class AdiVar:
+    """ADI with per-line coefficients (ntk_adi_var_* in include/ntk.h):
+    u_t = kx(y) u_xx + ky(x) u_yy, kx[j] on row j, ky[i] on column i
+    (float64 arrays of length N; kx = ky = 1 is Adi's step).
+
+    step(u, d_x, d_y) runs one Peaceman-Rachford step as run-adi.py:59-71
+    does: afterwards d_x holds the x half step, d_y the y half step and
+    u = d_y^T."""
+
+    def __init__(self, N, dx, dt, kx, ky, precision="fp64"):
+        import numpy as np
+
+        lib = load()
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        kxa = np.ascontiguousarray(kx, dtype=np.float64)
+        kya = np.ascontiguousarray(ky, dtype=np.float64)
+        if kxa.size != int(N) or kya.size != int(N):
+            raise ValueError("ntk: kx and ky need N values each")
+        h = ctypes.c_void_p()
+        check(lib.ntk_adi_var_create(ctypes.byref(h), int(N), float(dx), float(dt), kxa.ctypes.data,
+                                     kya.ctypes.data, prec))
+        self._h = h
+        self.N = int(N)
+
+    def step(self, u, d_x, d_y, stream=None):
+        check(load().ntk_adi_var_step(self._h, device_ptr(u), device_ptr(d_x), device_ptr(d_y), _stream(stream, u)))
+
+    def status(self, stream=None, raise_on_error=True):
+        flags = ctypes.c_int()
+        rc = load().ntk_adi_var_status(self._h, ctypes.byref(flags), _stream(stream, None))
+        if rc != _lib.NTK_ERR_RANGE or raise_on_error:
+            check(rc)
+        return flags.value
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            try:
+                load().ntk_adi_var_destroy(self._h)
             finally:
                 self._h = None
 

@@ -52,6 +52,7 @@ SIGNATURES = [
     ("ntk_solve", _i, [_vp, _vp, _vp]),
     ("ntk_solve_strided", _i, [_vp, _vp, _vp, _ll, _ll, _ll, _ll, _ll, _vp]),
     ("ntk_compact_deriv", _i, [_vp, _vp, _vp, _i, _i, _i, _i, _d, _vp]),
+    ("ntk_compact_grad", _i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _vp]),
     ("ntk_compact_rhs", _i, [_vp, _vp, _i, _i, _i, _d, _vp]),
     ("ntk_permute3d", _i, [_vp, _vp, _i, _i, _i, _ll, _ll, _ll, _vp]),
     ("ntk_adi_rhs", _i, [_vp, _vp, _i, _d, _d, _vp]),
@@ -62,6 +63,10 @@ SIGNATURES = [
     ("ntk_adi_segments", _i, [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     ("ntk_adi_step", _i, [_vp, _vp, _vp, _vp, _vp]),
     ("ntk_adi_run", _i, [_vp, _vp, _vp, _vp, _i, _i, _vp]),
+    ("ntk_adi_var_create", _i, [ctypes.POINTER(_vp), _i, _d, _d, _vp, _vp, _i]),
+    ("ntk_adi_var_destroy", _i, [_vp]),
+    ("ntk_adi_var_step", _i, [_vp, _vp, _vp, _vp, _vp]),
+    ("ntk_adi_var_status", _i, [_vp, ctypes.POINTER(_i), _vp]),
     ("ntk_adi_step_static", _i, [_i, _d, _d, _vp, _vp, _vp, _vp]),
     ("ntk_batch_create", _i, [ctypes.POINTER(_vp), _ll, _vp, _vp, _vp, _vp, _vp, _i]),
     ("ntk_batch_destroy", _i, [_vp]),

@@ -322,6 +322,26 @@ def adi_step_exact(u, d_x, d_y, dx, dt):
         u[:, :] = d.T
 
 
+def adi_step_var_exact(u, d_x, d_y, dx, dt, kx, ky):
+    """experiments/run-adi.py:59-71 with per-line coefficients (the model of
+    ntk_adi_var_step: kx[j] on row j of the x operator, ky[i] on column i of
+    the y operator) and the long-double Thomas solve.  In place."""
+    N = u.shape[0]
+    kx = np.asarray(kx, dtype=np.float64)
+    ky = np.asarray(ky, dtype=np.float64)
+    rdx2 = 1. / (dx * dx)
+    for d, kst, kmat in ((d_x, ky, kx), (d_y, kx, ky)):
+        beta = kst * rdx2
+        bt = -beta
+        cen = 2 * (-1. / dt + beta)
+        d[1:-1, 1:-1] = bt[None, 1:-1] * u[:-2, 1:-1] + cen[None, 1:-1] * u[1:-1, 1:-1] + bt[None, 1:-1] * u[2:, 1:-1]
+        for j in range(1, N - 1):
+            c = kmat[j] * rdx2
+            a, b, cc = near_toeplitz_bands(N, (1., 0., c, -2. * (1. / dt + c), c, 0., 1.))
+            d[j, :] = thomas_ld(a, b, cc, d[j, :])
+        u[:, :] = d.T
+
+
 def rel_err(x, ref):
     """max |x - ref| / max |ref| (normwise relative error)."""
     x = np.asarray(x, dtype=np.float64)

@@ -160,3 +160,41 @@ def test_persistent_ctas_cycle_their_tile_buffers(cuda, r2emu, shape, axis):
     assert torch.equal(o0, o2)
     rc, xe = r2emu_solve(r2emu, _lines(f.cpu().numpy(), axis))
     assert rc == 0 and _bits_equal(_lines(o0.cpu().numpy(), axis), xe)
+
+
+@pytest.mark.parametrize("precision", ["fp32_refine", "fp32"])
+def test_one_launch_gradient_equals_three_derivatives(cuda, precision):
+    """ntk_compact_grad on a 512^3 field (one launch of the combined kernel)
+    gives the same bits as the three ntk_compact_deriv calls."""
+    import ntk
+
+    f = _field((N, N, N), seed=9, cuda=cuda)
+    g = [torch.empty_like(f) for _ in range(3)]
+    d = [torch.empty_like(f) for _ in range(3)]
+    with ntk.Plan(N, 0, COMPACT, precision=precision) as p:
+        p.compact_grad(f, g[0], g[1], g[2], h=H)
+        for k, axis in enumerate((2, 1, 0)):
+            p.compact_deriv(f, d[k], axis=axis, h=H)
+        assert p.status() == 0
+    torch.cuda.synchronize()
+    for k in range(3):
+        assert torch.equal(g[k], d[k]), k
+    del g, d, f
+    torch.cuda.empty_cache()
+
+
+def test_gradient_falls_back_to_three_calls(cuda, oracle):
+    """Other sizes and FP64 run the three derivatives one after another."""
+    import ntk
+
+    n = 64
+    f = _field((n, n, n), seed=4, cuda=cuda)
+    for prec, tol in (("fp64", 1e-13), ("fp32_refine", 1e-12)):
+        outs = [torch.empty_like(f) for _ in range(3)]
+        with ntk.Plan(n, 0, COMPACT, precision=prec) as p:
+            p.compact_grad(f, *outs, h=1.0 / (n - 1))
+        torch.cuda.synchronize()
+        fc = f.cpu().numpy()
+        for o, axis in zip(outs, (2, 1, 0)):
+            ref = oracle.banded_compact_deriv(fc, 1.0 / (n - 1), axis=axis)
+            assert oracle.rel_err(o.cpu().numpy(), ref) < tol, (prec, axis)
