@@ -91,8 +91,9 @@ int ntk_plan_create(ntk_plan** out, int n, long long nrhs, const double coeffs[7
  *                           NTK_TUNE_REFINE_W sets the systems per CTA of
  *                           contiguous layouts (4, 8 or 16).
  *   NTK_TUNE_REFINE_PREFETCH  the one-group strided kernel: a CTA prefetches
- *                           into L2 the tile the CTA resident 1 (default)
- *                           or 2 waves later will load; 0 none. */
+ *                           into L2 the tile the CTA resident p / 2 waves
+ *                           later will load, p = 0 (none) .. 4; default 2
+ *                           (one wave). */
 enum ntk_tune_key {
   NTK_TUNE_F64_X_VARIANT = 1,
   NTK_TUNE_F64_THREADS = 2,
@@ -189,8 +190,13 @@ typedef struct ntk_adi ntk_adi;
  *   NTK_FP32_REFINE  FP32 solve + one double-word refinement sweep per half
  *                    step, over overlapping 32M-row windows (M = 16, 8 or 4;
  *                    needs N >= 128, else NTK_ERR_UNSUPPORTED); matches the
- *                    FP64 path to ~1e-13.
- *   NTK_FP32         the same windows without the refinement sweep.
+ *                    FP64 path to ~1e-13.  Where the factors decay too slowly
+ *                    for the windows' halos (large dt / dx^2) and N > 512:
+ *                    the reference's six kernels per step with an exact
+ *                    partitioned FP32 solve (512-row partitions coupled by a
+ *                    reduced system, two sweeps; N <= 8192) and an N x N
+ *                    work array.
+ *   NTK_FP32         the same without the refinement sweeps.
  * Synchronous. */
 int ntk_adi_create(ntk_adi** out, int N, double dx, double dt, int precision);
 
@@ -202,8 +208,9 @@ int ntk_adi_status(ntk_adi* adi, int* flags, void* stream);
 
 /* The segmentation the plan chose: for windows (NTK_FP32, NTK_FP32_REFINE,
  * and NTK_FP64 where they apply) the windows' central rows, halo and windows
- * per system; for the segmented FP64 sweeps segment length, halo and
- * segments per system (1 segment = plain sweeps). */
+ * per system; for the partitioned FP32 solve 512, 0 and the partitions per
+ * system; for the segmented FP64 sweeps segment length, halo and segments
+ * per system (1 segment = plain sweeps). */
 int ntk_adi_segments(const ntk_adi* adi, int* seg_len, int* halo, int* nseg);
 
 /* One time step on device arrays u, d_x, d_y (N x N, C order), with the

@@ -17,6 +17,12 @@
 // enough for a halo exact to rounding (r = 0.5: |l| -> 0.268, 36 rows);
 // otherwise the segmented FP64 sweeps (ntk_solve_f64.cu) with the largest
 // exact segmentation.
+// In FP32 + refinement the half steps solve overlapping windows as well
+// (ntk_adi_refine.cu); where their factors decay too slowly for an exact
+// halo (large r), a step runs the reference's six kernels instead, with the
+// partitioned FP32 solve of ntk_spike.cu (nothing truncated) for the rows:
+// stencil into d_x, solve, transpose into u, stencil into a work array
+// carrying d_y's boundary, solve, transpose into u.
 // A whole run of steps can be captured once in a CUDA graph and replayed.
 #include <cmath>
 #include <cstring>
@@ -28,6 +34,7 @@
 #include "ntk_adi_refine.h"
 #include "ntk_internal.h"
 #include "ntk_plan.h"
+#include "ntk_spike.h"
 
 namespace ntk {
 
@@ -41,6 +48,7 @@ struct Adi {
   double bottom = 0, center = 0, top = 0;
   AdiRefine* refine = nullptr;  // NTK_FP32 / NTK_FP32_REFINE half steps (ntk_adi_refine.cu)
   AdiF64* windows = nullptr;    // NTK_FP64 window half steps (ntk_adi_f64.cu), else segmented sweeps
+  SpikeSolver* spike = nullptr;  // FP32 / FP32 + refinement rows where the windows do not apply
   cudaStream_t capture_stream = nullptr;
   std::map<std::tuple<const void*, const void*, const void*, int>, cudaGraphExec_t> graphs;
 
@@ -50,6 +58,7 @@ struct Adi {
     if (scratch) cudaFree(scratch);
     if (refine) adi_refine_destroy(refine);
     if (windows) adi_f64_destroy(windows);
+    if (spike) spike_destroy(spike);
   }
 };
 
@@ -59,7 +68,50 @@ namespace {
 // window [(g+1)L, (g+1)L+H) has a factor product below 2^-64.
 }  // namespace
 
+namespace {
+
+// The boundary of the y half step's work array w, which the final
+// transpose turns into u's boundary: rows 0 and N-1 of w are u's columns 0
+// and N-1 as they are before the step (so they are not rewritten), columns
+// 0 and N-1 of w's rows 1..N-2 are d_y's (the y systems' identity rows).
+__global__ void adi_boundary_kernel(const double* __restrict__ u, const double* __restrict__ d_y,
+                                    double* __restrict__ w, int N) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const long long row = (long long)i * N;
+  w[i] = u[row];
+  w[(long long)(N - 1) * N + i] = u[row + N - 1];
+  if (i > 0 && i < N - 1) {
+    w[row] = d_y[row];
+    w[row + N - 1] = d_y[row + N - 1];
+  }
+}
+
+// experiments/run-adi.py:59-71 with the partitioned FP32 + refinement
+// solve: rows 1 .. N-2 of d_x, then of the work array
+int adi_spike_step(Adi* a, double* u, double* d_x, const double* d_y, cudaStream_t st) {
+  const int N = a->N;
+  Batch rows;
+  rows.nsys = N - 2;
+  rows.ni = N - 2;
+  rows.is = N;
+  rows.os = 0;
+  rows.es = 1;
+  adi_boundary_kernel<<<(N + 255) / 256, 256, 0, st>>>(u, d_y, a->scratch, N);
+  int rc = cuda_status(cudaGetLastError(), "adi_boundary_kernel");
+  if (!rc) rc = launch_adi_rhs(u, d_x, N, a->bottom, a->center, a->top, st);
+  if (!rc) rc = spike_solve(a->spike, d_x + N, d_x + N, rows, st);
+  if (!rc) rc = launch_transpose2d(d_x, u, N, st);
+  if (!rc) rc = launch_adi_rhs(u, a->scratch, N, a->bottom, a->center, a->top, st);
+  if (!rc) rc = spike_solve(a->spike, a->scratch + N, a->scratch + N, rows, st);
+  if (!rc) rc = launch_transpose2d(a->scratch, u, N, st);
+  return rc;
+}
+
+}  // namespace
+
 int adi_step(Adi* a, double* u, double* d_x, const double* d_y, cudaStream_t st) {
+  if (a->spike) return adi_spike_step(a, u, d_x, d_y, st);
   if (a->refine) return adi_refine_step(a->refine, u, d_x, d_y, st);
   if (a->windows) return adi_f64_step(a->windows, u, d_x, d_y, st);
   const int N = a->N;
@@ -148,6 +200,14 @@ int ntk_adi_create(ntk_adi** out, int N, double dx, double dt, int precision) {
         rc = ntk::cuda_status(cudaMalloc(&a->scratch, sizeof(double) * (size_t)N * N), "cudaMalloc(ADI scratch)");
     } else {
       rc = ntk::adi_refine_create(&a->refine, N, dx, dt, precision);
+      if (rc == NTK_ERR_UNSUPPORTED && N > 512) {
+        // windows would truncate: exact partitions, the reference's kernel
+        // sequence, and two sweeps for the badly conditioned matrices that
+        // decay this slowly
+        rc = ntk::spike_create(&a->spike, a->plan.mat, precision == NTK_FP32 ? 0 : 2);
+        if (!rc)
+          rc = ntk::cuda_status(cudaMalloc(&a->scratch, sizeof(double) * (size_t)N * N), "cudaMalloc(ADI work)");
+      }
     }
   }
   if (rc) {
@@ -170,6 +230,7 @@ int ntk_adi_status(ntk_adi* adi, int* flags, void* stream) {
   }
   std::vector<unsigned*> words;
   ntk::adi_refine_status_words(adi->refine, words);
+  ntk::spike_status_words(adi->spike, words);
   return ntk::read_clear_status(words, (cudaStream_t)stream, flags);
 }
 
@@ -177,6 +238,13 @@ int ntk_adi_segments(const ntk_adi* adi, int* seg_len, int* halo, int* nseg) {
   if (!adi) {
     ntk::set_error("ntk_adi_segments: null plan");
     return NTK_ERR_INVALID;
+  }
+  if (adi->spike) {
+    // partitions of 512 rows, no halo
+    if (seg_len) *seg_len = 512;
+    if (halo) *halo = 0;
+    if (nseg) *nseg = ntk::spike_partitions(adi->spike);
+    return NTK_OK;
   }
   if (adi->refine || adi->windows) {
     // windows: central rows per window, halo, windows per system

@@ -257,7 +257,7 @@ int ntk_plan_set_tuning(ntk_plan* plan, int key, int value) {
       plan->tune_refine_kernel = value;
       return NTK_OK;
     case NTK_TUNE_REFINE_PREFETCH:
-      if (value < 0 || value > 2) break;
+      if (value < 0 || value > 4) break;
       plan->tune_refine_prefetch = value;
       return NTK_OK;
     default:

@@ -56,6 +56,7 @@ bool factor_host(const Matrix& m, std::vector<double>& l, std::vector<double>& u
 
 struct RefineState;  // ntk_refine.cu
 struct LongRefine;   // ntk_long_refine.cu
+struct SpikeSolver;  // ntk_spike.cu
 
 struct Plan {
   int n = 0;
@@ -70,6 +71,7 @@ struct Plan {
   std::map<double, double*> g_by_scale;  // device g = s/u per RHS scale
   RefineState* refine = nullptr;
   LongRefine* long_refine = nullptr;  // FP32 / FP32+refine windows for n > 1024
+  SpikeSolver* spike = nullptr;       // n > 1024 where the windows' halos do not decay: exact partitions
   std::mutex mu;
   // launch configuration (ntk_plan_set_tuning; chosen by the autotuner)
   int tune_f64_x_variant = 0;  // contiguous FP64 sweeps: 0 tile ring, 1 whole-system tile, 2 direct
@@ -78,7 +80,7 @@ struct Plan {
   int tune_refine_spw = 1;     // systems per warp (2: strided layouts, 16 rows per lane)
   int tune_refine_kernel = 0;  // n = 512: paired-chunk TMA kernels where they apply (0: automatic, 2: one
                                // strided group per CTA, 3: persistent strided CTAs), 1: the chunked kernel
-  int tune_refine_prefetch = 1;  // one-group strided CTAs: L2 prefetch 0, 1 or 2 waves ahead
+  int tune_refine_prefetch = 2;  // one-group strided CTAs: L2 prefetch 0 .. 4 half waves ahead
 
   int init(int n, long long nrhs, const double co[7], int precision, int sweeps);
   ~Plan();

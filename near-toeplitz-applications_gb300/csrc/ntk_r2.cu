@@ -20,8 +20,9 @@
 // Each thread: compact RHS (one FP64 subtraction per row) split into a
 // double-word, the FP32 solve of the pure Toeplitz factors with the Woodbury
 // end corrections, the exact double-word residual, the FP32 correction
-// solve, and the FP64 output assembled with integer operations, written in
-// place into the tile; one TMA store writes the tile back.  Out-of-range
+// solve, and the FP64 output assembled with integer operations: written in
+// place into the tile and stored by TMA for contiguous systems, stored from
+// registers (128-byte row segments per half-warp) for strided ones.  Out-of-range
 // inputs raise a status bit; a bounded wait on the TMA barrier that runs out
 // raises another and skips the group.
 #include <cuda.h>
@@ -340,14 +341,32 @@ constexpr size_t S_SMEM = 1024 + S_TILE_BYTES + S_XCH_FLOATS * 4 + 16;
 constexpr int P_BUFS = 3;
 constexpr size_t P_SMEM = 1024 + P_BUFS * S_TILE_BYTES + 2 * S_XCH_FLOATS * 4 + 8 * P_BUFS + 8;
 
-// One group of 16 systems, solved in place in its [512][16] tile by 512
-// threads: thread t owns system t % 16 and chunk t / 16.  The first and
-// last rows of a chunk are the halo rows its neighbours read for the compact
-// RHS, so they are rewritten only after the first barrier; every other row
-// is rewritten as soon as it is formed.  Returns the thread's largest input
-// magnitude (high word) for the range check.
-template <int RHS, int SWEEPS, class SYNC>
-__device__ __forceinline__ unsigned strided_group(double* tile, float* xch, int t, const Args& a, SYNC sync) {
+// Where a strided group's results go: element (system x, row r, plane p) at
+// p + plane * ps + x + r * es; systems at or beyond ni (a partial group) are
+// not stored.
+struct OutDesc {
+  double* p;
+  long long es, ps;
+  int ni;
+};
+// Row r0 of system x0 + s of `plane`, or null beyond the last system.
+__device__ __forceinline__ double* out_row(const OutDesc& o, int x0, int plane, int s, int r0) {
+  return x0 + s < o.ni ? o.p + (long long)plane * o.ps + (x0 + s) + (long long)r0 * o.es : nullptr;
+}
+
+// One group of 16 systems in its [512][16] tile, solved by 512 threads:
+// thread t owns system t % 16 and chunk t / 16.  DIRECT: the thread stores
+// its 16 results from registers to out_of() (row r0 of its system, or null:
+// nothing to store), rows es apart, a half-warp writing one 128-byte row
+// segment; otherwise they are written in place into the tile.  With
+// refinement the (hi, lo) split of each RHS row is kept in the tile for the
+// residual; the first and last rows of a chunk are the halo rows its
+// neighbours read for the compact RHS, so they are rewritten only after the
+// first barrier.  Returns the thread's largest input magnitude (high word)
+// for the range check.
+template <int RHS, int SWEEPS, bool DIRECT, class SYNC, class OUTF>
+__device__ __forceinline__ unsigned strided_group(double* tile, float* xch, int t, const Args& a, SYNC sync,
+                                                  OUTF out_of, long long es) {
   const int s = t & 15;
   const int c = t >> 4;
   const int r0 = ROWS * c;
@@ -378,9 +397,11 @@ __device__ __forceinline__ unsigned strided_group(double* tile, float* xch, int 
         h = bh;
         l = bl;
       }
-      if (k == 0) edge0 = make_float2(h, l);
-      else if (k == ROWS - 1) edge15 = make_float2(h, l);
-      else reinterpret_cast<float2*>(col + (r0 + k) * SG)[0] = make_float2(h, l);
+      if (SWEEPS > 0) {
+        if (k == 0) edge0 = make_float2(h, l);
+        else if (k == ROWS - 1) edge15 = make_float2(h, l);
+        else reinterpret_cast<float2*>(col + (r0 + k) * SG)[0] = make_float2(h, l);
+      }
       if (k < HALF) v[k].x = h;
       else v[k - HALF].y = h;
       prev = cur;
@@ -391,7 +412,7 @@ __device__ __forceinline__ unsigned strided_group(double* tile, float* xch, int 
     for (int k = 0; k < ROWS; ++k) {
       float h, l;
       split_f64(col[(r0 + k) * SG], h, l, rmax);
-      reinterpret_cast<float2*>(col + (r0 + k) * SG)[0] = make_float2(h, l);
+      if (SWEEPS > 0) reinterpret_cast<float2*>(col + (r0 + k) * SG)[0] = make_float2(h, l);
       if (k < HALF) v[k].x = h;
       else v[k - HALF].y = h;
     }
@@ -399,7 +420,7 @@ __device__ __forceinline__ unsigned strided_group(double* tile, float* xch, int 
   // ---- FP32 solve ----
   X(X_E1, c) = fwd_local(v, K);
   sync();  // carries published; every halo row has been read
-  if (RHS == RHS_COMPACT) {
+  if (RHS == RHS_COMPACT && SWEEPS > 0) {
     reinterpret_cast<float2*>(col + r0 * SG)[0] = edge0;
     reinterpret_cast<float2*>(col + (r0 + ROWS - 1) * SG)[0] = edge15;
   }
@@ -414,12 +435,16 @@ __device__ __forceinline__ unsigned strided_group(double* tile, float* xch, int 
   if (c == 0) head_fix(v, K);
   if (c == CHUNKS - 1) tail_fix(v, K);
   if (SWEEPS == 0) {
+    double* out = DIRECT ? out_of() : col + r0 * SG;
+    const long long step = DIRECT ? es : SG;
+    if (out) {
 #pragma unroll
-    for (int k = 0; k < HALF; ++k) {
-      double oa, ob;
-      out_pair0(v[k], a, oa, ob);
-      col[(r0 + k) * SG] = oa;
-      col[(r0 + k + HALF) * SG] = ob;
+      for (int k = 0; k < HALF; ++k) {
+        double oa, ob;
+        out_pair0(v[k], a, oa, ob);
+        out[k * step] = oa;
+        out[(k + HALF) * step] = ob;
+      }
     }
     return rmax;
   }
@@ -475,12 +500,16 @@ __device__ __forceinline__ unsigned strided_group(double* tile, float* xch, int 
   bwd_fix(r, c < CHUNKS - 1 ? X(X_S2, c + 1) : 0.f, K);
   if (c == 0) head_fix(r, K);
   if (c == CHUNKS - 1) tail_fix(r, K);
+  double* out = DIRECT ? out_of() : col + r0 * SG;
+  const long long step = DIRECT ? es : SG;
+  if (out) {
 #pragma unroll
-  for (int k = 0; k < HALF; ++k) {
-    double oa, ob;
-    out_pair(v[k], r[k], a, oa, ob);
-    col[(r0 + k) * SG] = oa;
-    col[(r0 + k + HALF) * SG] = ob;
+    for (int k = 0; k < HALF; ++k) {
+      double oa, ob;
+      out_pair(v[k], r[k], a, oa, ob);
+      out[k * step] = oa;
+      out[(k + HALF) * step] = ob;
+    }
   }
   return rmax;
 }
@@ -491,13 +520,12 @@ __device__ __forceinline__ void group_coords(int g, int gpp, int& x0, int& plane
   x0 = (g - plane * gpp) * SG;
 }
 
-// One group per CTA.
 // One 16-system strided group per CTA, boxes at (x0, 0 | 256, plane, 0):
-// load, solve, store.  prefetch() runs on thread 0 once its own load is
-// issued.
+// load, solve, store from registers.  prefetch() runs on thread 0 once its
+// own load is issued.
 template <int RHS, int SWEEPS, class PF>
 __device__ __forceinline__ void strided_cta(double* tile, float* xch, uint64_t* bar, const CUtensorMap* tin,
-                                            const CUtensorMap* tout, int x0, int plane, const Args& a, PF prefetch) {
+                                            const OutDesc& o, int x0, int plane, const Args& a, PF prefetch) {
   const int tid = threadIdx.x;
   if (tid == 0) mbar_init(bar, 1);
   __syncthreads();
@@ -511,15 +539,9 @@ __device__ __forceinline__ void strided_cta(double* tile, float* xch, uint64_t* 
     if (tid == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
     return;
   }
-  const unsigned rmax = strided_group<RHS, SWEEPS>(tile, xch, tid, a, SyncAll());
+  const unsigned rmax = strided_group<RHS, SWEEPS, true>(
+      tile, xch, tid, a, SyncAll(), [&] { return out_row(o, x0, plane, tid & 15, ROWS * (tid >> 4)); }, o.es);
   if (__any_sync(FULL, rmax >= RANGE_MAG) && (tid & 31) == 0 && a.status) atomicOr(a.status, 1u);
-  fence_proxy_async();
-  __syncthreads();
-  if (tid == 0) {
-    tma_store(tout, x0, 0, plane, 0, tile);
-    tma_store(tout, x0, NROWS / 2, plane, 0, tile + (NROWS / 2) * SG);
-    tma_store_commit_and_wait();
-  }
 }
 
 // pf_dist > 0: on starting, a CTA prefetches into L2 the tile of the group
@@ -527,7 +549,7 @@ __device__ __forceinline__ void strided_cta(double* tile, float* xch, uint64_t* 
 // the number of CTAs resident at once), so that load is served from L2.
 template <int RHS, int SWEEPS>
 __global__ void __launch_bounds__(512, 2)
-    r2s_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout,
+    r2s_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ OutDesc o,
                const __grid_constant__ Args a, int gpp, int pf_dist) {
   extern __shared__ unsigned char smem_raw[];
   double* tile = reinterpret_cast<double*>(align1024(smem_raw));  // [512][16]
@@ -535,7 +557,7 @@ __global__ void __launch_bounds__(512, 2)
   uint64_t* bar = reinterpret_cast<uint64_t*>(xch + S_XCH_FLOATS);
   int x0, plane;
   group_coords(blockIdx.x, gpp, x0, plane);
-  strided_cta<RHS, SWEEPS>(tile, xch, bar, &tin, &tout, x0, plane, a, [&] {
+  strided_cta<RHS, SWEEPS>(tile, xch, bar, &tin, o, x0, plane, a, [&] {
     const long long gn = (long long)blockIdx.x + pf_dist;
     if (pf_dist > 0 && gn < (long long)gridDim.x) {
       int px, pp;
@@ -555,7 +577,8 @@ __global__ void __launch_bounds__(512, 2)
 // for the other -- and after all planes the z CTAs (gz, 16 columns each).
 struct GradGeom {
   int nz, cx, cy, gz;
-  int pf;  // prefetch distance in CTAs (0: none)
+  int pf;        // prefetch distance in CTAs (0: none)
+  OutDesc y, z;  // outputs of the y and z derivatives
 };
 constexpr int GX_SUB = 4;  // systems per x sub-group (one 128-thread group)
 constexpr size_t G_SMEM = S_SMEM > 1024 + (size_t)4 * GX_SUB * NROWS * 8 + 4 * GX_SUB * 16 + 4 * 8 + 16
@@ -583,8 +606,7 @@ __device__ __forceinline__ void grad_prefetch(const CUtensorMap* mx, const CUten
 template <int SWEEPS>
 __global__ void __launch_bounds__(512, 2)
     r2g_kernel(const __grid_constant__ CUtensorMap fx, const __grid_constant__ CUtensorMap ox,
-               const __grid_constant__ CUtensorMap fy, const __grid_constant__ CUtensorMap oy,
-               const __grid_constant__ CUtensorMap fz, const __grid_constant__ CUtensorMap oz,
+               const __grid_constant__ CUtensorMap fy, const __grid_constant__ CUtensorMap fz,
                const __grid_constant__ Args ax, const __grid_constant__ GradGeom g) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = align1024(smem_raw);
@@ -612,23 +634,23 @@ __global__ void __launch_bounds__(512, 2)
       double* tile = reinterpret_cast<double*>(base);
       float* xch = reinterpret_cast<float*>(tile + NROWS * SG);
       uint64_t* bar = reinterpret_cast<uint64_t*>(xch + S_XCH_FLOATS);
-      strided_cta<RHS_COMPACT, SWEEPS>(tile, xch, bar, &fy, &oy, (r - g.cx) * SG, p, ax, prefetch);
+      strided_cta<RHS_COMPACT, SWEEPS>(tile, xch, bar, &fy, g.y, (r - g.cx) * SG, p, ax, prefetch);
     }
   } else {
     double* tile = reinterpret_cast<double*>(base);
     float* xch = reinterpret_cast<float*>(tile + NROWS * SG);
     uint64_t* bar = reinterpret_cast<uint64_t*>(xch + S_XCH_FLOATS);
-    strided_cta<RHS_COMPACT, SWEEPS>(tile, xch, bar, &fz, &oz, (int)(b - nxy) * SG, 0, ax, prefetch);
+    strided_cta<RHS_COMPACT, SWEEPS>(tile, xch, bar, &fz, g.z, (int)(b - nxy) * SG, 0, ax, prefetch);
   }
 }
 
 // Persistent CTA (one per SM, 1024 threads): its groups are blockIdx.x +
 // k * gridDim.x, k = 0, 1, ...; half h (512 threads) solves k = h, h + 2, ...
-// in tile buffer k % 3.  The half that finishes group k stores it, and once
-// the store has read the tile it loads group k + 3 into the same buffer for
-// the other half, so one tile is always loading while two are in compute.
-// Each buffer's mbarrier completes once per load: load n of buffer b is
-// waited on with parity n & 1.
+// in tile buffer k % 3, in place.  The half that finishes group k stores it
+// by TMA, and once the store has read the tile it loads group k + 3 into the
+// same buffer for the other half, so one tile is always loading while two
+// are in compute.  Each buffer's mbarrier completes once per load: load n of
+// buffer b is waited on with parity n & 1.
 __device__ __forceinline__ void load_group(double* buf, uint64_t* bar, const CUtensorMap* map, int g, int gpp) {
   int x0, plane;
   group_coords(g, gpp, x0, plane);
@@ -704,7 +726,8 @@ __global__ void __launch_bounds__(1024, 1)
       if (t == 0 && a.status) atomicOr(a.status, STATUS_TIMEOUT);
       return;
     }
-    const unsigned rmax = strided_group<RHS, SWEEPS>(tile, sm.xch + h * S_XCH_FLOATS, t, a, sync);
+    const unsigned rmax = strided_group<RHS, SWEEPS, false>(tile, sm.xch + h * S_XCH_FLOATS, t, a, sync,
+                                                           [] { return (double*)nullptr; }, 0);
     if (__any_sync(FULL, rmax >= RANGE_MAG) && (t & 31) == 0 && a.status) atomicOr(a.status, 1u);
     fence_proxy_async();
     if (t == 0) sm.knext[h] = k + 2;
@@ -793,9 +816,8 @@ int launch_s(const double* in, double* out, const Batch& b, const Args& a, bool 
   const long long ps = nplanes > 1 ? b.os : b.es * NROWS;
   const cuuint64_t strides[3] = {(cuuint64_t)b.es * 8, (cuuint64_t)ps * 8, (cuuint64_t)ps * nplanes * 8};
   const cuuint32_t box[4] = {(cuuint32_t)SG, (cuuint32_t)(NROWS / 2), 1, 1};
-  CUtensorMap mi, mo;
+  CUtensorMap mi;
   int rc = encode(&mi, in, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE);
-  if (!rc) rc = encode(&mo, out, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE);
   if (rc) return rc;
   const long long gpp = (ni + SG - 1) / SG;
   const long long grid = gpp * nplanes;
@@ -811,11 +833,16 @@ int launch_s(const double* in, double* out, const Batch& b, const Args& a, bool 
     auto kern = r2s_kernel<RHS, SWEEPS>;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_SMEM);
     if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2s_kernel)");
-    // two 512-thread CTAs per SM fill its registers: a wave is 2 * SMs groups
-    const int pf = prefetch * 2 * sms;
+    // two 512-thread CTAs per SM fill its registers: a wave is 2 * SMs
+    // groups, prefetch counts half waves
+    const int pf = prefetch * sms;
+    const OutDesc mo{out, b.es, ps, (int)ni};
     kern<<<(unsigned)grid, 32 * CHUNKS / 2, S_SMEM, st>>>(mi, mo, a, (int)gpp, pf);
     return cuda_status(cudaGetLastError(), "r2s_kernel");
   }
+  CUtensorMap mo;
+  rc = encode(&mo, out, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if (rc) return rc;
   auto kern = r2sp_kernel<RHS, SWEEPS>;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P_SMEM);
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2sp_kernel)");
@@ -862,13 +889,11 @@ int launch_grad(const double* f, double* ox, double* oy, double* oz, const Args&
   const cuuint64_t dz[4] = {n * n, n, 1, 1};
   const cuuint64_t sz[3] = {n * n * 8, n * n * n * 8, n * n * n * 8};
   const cuuint32_t bs[4] = {(cuuint32_t)SG, (cuuint32_t)(NROWS / 2), 1, 1};
-  CUtensorMap m[6];
+  CUtensorMap m[4];
   int rc = encode(&m[0], f, dx, sx, bx, CU_TENSOR_MAP_SWIZZLE_128B);
   if (!rc) rc = encode(&m[1], ox, dx, sx, bx, CU_TENSOR_MAP_SWIZZLE_128B);
   if (!rc) rc = encode(&m[2], f, dy, sy, bs, CU_TENSOR_MAP_SWIZZLE_NONE);
-  if (!rc) rc = encode(&m[3], oy, dy, sy, bs, CU_TENSOR_MAP_SWIZZLE_NONE);
-  if (!rc) rc = encode(&m[4], f, dz, sz, bs, CU_TENSOR_MAP_SWIZZLE_NONE);
-  if (!rc) rc = encode(&m[5], oz, dz, sz, bs, CU_TENSOR_MAP_SWIZZLE_NONE);
+  if (!rc) rc = encode(&m[3], f, dz, sz, bs, CU_TENSOR_MAP_SWIZZLE_NONE);
   if (rc) return rc;
   int dev = 0, sms = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -879,12 +904,14 @@ int launch_grad(const double* f, double* ox, double* oy, double* oz, const Args&
   g.cx = NROWS / 16;
   g.cy = NROWS / SG;
   g.gz = NROWS * NROWS / SG;
-  g.pf = prefetch * 2 * sms;
+  g.pf = prefetch * sms;
+  g.y = OutDesc{oy, (long long)n, (long long)(n * n), (int)n};
+  g.z = OutDesc{oz, (long long)(n * n), 0, (int)(n * n)};
   const long long grid = (long long)g.nz * (g.cx + g.cy) + g.gz;
   auto kern = sweeps ? r2g_kernel<1> : r2g_kernel<0>;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM);
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(r2g_kernel)");
-  kern<<<(unsigned)grid, 512, G_SMEM, st>>>(m[0], m[1], m[2], m[3], m[4], m[5], a, g);
+  kern<<<(unsigned)grid, 512, G_SMEM, st>>>(m[0], m[1], m[2], m[3], a, g);
   return cuda_status(cudaGetLastError(), "r2g_kernel");
 }
 

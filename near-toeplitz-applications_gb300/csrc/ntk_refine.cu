@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "ntk_long_refine.h"
+#include "ntk_spike.h"
 #include "ntk_r2.h"
 #include "ntk_refine.cuh"
 
@@ -59,8 +60,12 @@ int Plan::init_refine() {
     }
   if (M == 0) {
     // longer than one warp's register tile: overlapping windows
-    // (ntk_long_refine.cu); the plan keeps no per-row tables of its own
-    return long_refine_create(&long_refine, *this, precision, sweeps);
+    // (ntk_long_refine.cu); where the LU multipliers decay too slowly for
+    // their halos, exact partitions coupled by a reduced system
+    // (ntk_spike.cu); the plan keeps no per-row tables of its own
+    const int rc = long_refine_create(&long_refine, *this, precision, sweeps);
+    if (rc != NTK_ERR_UNSUPPORTED) return rc;
+    return spike_create(&spike, mat, precision == NTK_FP32 ? 0 : sweeps);
   }
   st->M = M;
   st->n_pad = 32 * M;
@@ -180,12 +185,17 @@ int Plan::init_refine() {
 void Plan::status_words(std::vector<unsigned*>& out) const {
   if (refine && refine->d_status) out.push_back(refine->d_status);
   if (long_refine) long_refine_status_words(long_refine, out);
+  if (spike) spike_status_words(spike, out);
 }
 
 void Plan::release_refine() {
   if (long_refine) {
     long_refine_destroy(long_refine);
     long_refine = nullptr;
+  }
+  if (spike) {
+    spike_destroy(spike);
+    spike = nullptr;
   }
   if (!refine) return;
   if (refine->d_tab) cudaFree(refine->d_tab);
@@ -196,6 +206,13 @@ void Plan::release_refine() {
 
 int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsParams& rp, double s,
                      cudaStream_t stream) {
+  if (spike) {
+    if (rp.kind != RHS_IDENTITY || s != 1.0) {
+      set_error("FP32/refine with slowly decaying LU factors (n > 1024) supports the plain solve only");
+      return NTK_ERR_UNSUPPORTED;
+    }
+    return spike_solve(spike, in, out, b, stream);
+  }
   if (long_refine) {
     if (rp.kind != RHS_IDENTITY && rp.kind != RHS_COMPACT) {
       set_error("FP32/refine supports the identity and compact right-hand sides");

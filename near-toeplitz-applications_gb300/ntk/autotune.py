@@ -18,8 +18,9 @@ cached per (device, kernel family, n, precision, layout):
                  refine_w = systems per CTA of contiguous layouts) with one
                  strided group per CTA (2) or persistent strided CTAs (3);
                  1 the chunked kernel (refine_w, refine_spw as above)
-  refine_prefetch  one-group strided CTAs: L2 prefetch of the tile needed 0,
-                 1 or 2 waves later
+  refine_prefetch  one-group strided CTAs: L2 prefetch of the tile needed
+                 p / 2 waves later (p = 1, 2, 3 searched; 0 and 4, no
+                 prefetch and two waves, measured slower on every axis)
 
 Usage:
     best = autotune.tune(plan, run, key)   # run() launches the workload once
@@ -35,10 +36,10 @@ _lock = threading.Lock()
 
 SPACE = {
     "fp64": [{"f64_x_variant": [0, 1], "f64_threads": [64, 128]}],
-    "fp32": [{"refine_kernel": [2], "refine_w": [4, 8, 16], "refine_prefetch": [0, 1, 2]},
+    "fp32": [{"refine_kernel": [2], "refine_w": [4, 8, 16], "refine_prefetch": [1, 2, 3]},
              {"refine_kernel": [3], "refine_w": [4, 8, 16]},
              {"refine_kernel": [1], "refine_w": [4, 8, 16], "refine_spw": [1, 2]}],
-    "fp32_refine": [{"refine_kernel": [2], "refine_w": [4, 8, 16], "refine_prefetch": [0, 1, 2]},
+    "fp32_refine": [{"refine_kernel": [2], "refine_w": [4, 8, 16], "refine_prefetch": [1, 2, 3]},
                     {"refine_kernel": [3], "refine_w": [4, 8, 16]},
                     {"refine_kernel": [1], "refine_w": [4, 8, 16], "refine_spw": [1, 2]}],
 }

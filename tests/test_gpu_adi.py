@@ -179,11 +179,13 @@ def test_adi_fp32_only_error_is_reported_scale(cuda, oracle):
 
 
 def test_adi_refine_rejects_slow_decay_windows(cuda):
-    """r = 40 at N = 2048: the halo the 2^-56 truncation needs leaves too few
-    central rows per 512-row window; the plan says so instead of running."""
+    """r = 40 at N = 300: the halo the 2^-56 truncation needs leaves no
+    central rows in a 256-row window, and systems this short have no
+    partitioned fallback (N > 512 has one, tests/test_gpu_spike.py); the
+    plan says so instead of running."""
     import ntk
 
-    N = 2048
+    N = 300
     dx = 1.0 / (N - 1)
     with pytest.raises(Exception) as ei:
         ntk.Adi(N, dx, 80 * dx * dx, precision="fp32_refine")
