@@ -29,6 +29,7 @@
 
 #include "ntk_adi_geom.h"
 #include "ntk_adi_refine.h"
+#include "ntk_r2_adi.h"
 #include "ntk_refine.cuh"
 
 namespace ntk {
@@ -209,14 +210,17 @@ struct AdiRefine {
   RefineArgs* d_args = nullptr;  // kernel arguments of the four kinds (device)
   int max_ncls = 1;
   bool pow2 = true, decay = true;
+  r2::AdiR2* r2a = nullptr;  // the paired-chunk half steps (ntk_r2_adi.cu) where they apply
   ~AdiRefine() {
     if (d_args) cudaFree(d_args);
+    if (r2a) r2::adi_destroy(r2a);
   }
 };
 
 void adi_refine_status_words(const AdiRefine* ar, std::vector<unsigned*>& out) {
   if (!ar) return;
   for (const Plan& w : ar->win) w.status_words(out);
+  r2::adi_status_words(ar->r2a, out);
 }
 
 int adi_refine_create(AdiRefine** out, int N, double dx, double dt, int precision) {
@@ -276,6 +280,24 @@ int adi_refine_create(AdiRefine** out, int N, double dx, double dt, int precisio
   // [gL - H, gL + L + H); last [N - Lw, N) writes [(P-1) L, N)
   const int Pm1 = (N - ar->Lw + ar->H + ar->L - 1) / ar->L;  // ceil((N - Lw + H) / L)
   ar->P = ar->whole ? 1 : (Pm1 < 1 ? 1 : Pm1) + 1;
+  // the paired-chunk kernels (ntk_r2_adi.cu: 512-row windows, power-of-two
+  // interior, at most one sweep): their TMA boxes start on 16-row
+  // boundaries, so the halo is rounded up to a multiple of 16
+  if (ar->M == 16 && ar->sweeps <= 1) {
+    const int H16 = ar->whole ? ar->H : (ar->H + 15) & ~15;
+    const int L16 = ar->whole ? ar->Lw : ar->Lw - 2 * H16;
+    if (ar->whole || L16 >= ar->Lw / 4) {
+      const int Q = (N - ar->Lw + H16 + L16 - 1) / L16;
+      const int P16 = ar->whole ? 1 : (Q < 1 ? 1 : Q) + 1;
+      std::string why;
+      ar->r2a = r2::adi_create(N, L16, H16, P16, ar->whole, beta, ar->gamma, ar->sweeps, &why);
+      if (ar->r2a) {
+        ar->H = H16;
+        ar->L = L16;
+        ar->P = P16;
+      }
+    }
+  }
   // scaled rows: coeffs (b1, c1, ai, bi, ci, an, bn)
   const double first[7] = {1.0, 0.0, 1.0, beta, 1.0, 1.0, beta};
   const double middle[7] = {beta, 1.0, 1.0, beta, 1.0, 1.0, beta};
@@ -361,6 +383,7 @@ int half_step(AdiRefine* ar, const double* in, double* out, long long is, long l
 }  // namespace
 
 int adi_refine_step(AdiRefine* ar, double* u, double* d_x, const double* d_y, cudaStream_t st) {
+  if (ar->r2a) return r2::adi_step(ar->r2a, u, d_x, d_y, ar->wx, st);
   const int N = ar->N;
   // x half: systems = rows 1..N-2, stencil of u's rows, boundary RHS from d_x
   int rc = half_step(ar, u + N, d_x + N, N, 1, d_x + N, N, 1, ar->wx, st);

@@ -25,106 +25,18 @@
 // registers (128-byte row segments per half-warp) for strided ones.  Out-of-range
 // inputs raise a status bit; a bounded wait on the TMA barrier that runs out
 // raises another and skips the group.
-#include <cuda.h>
-
-#include <mutex>
-
 #include "ntk_internal.h"
 #include "ntk_plan.h"
 #include "ntk_r2.h"
+#include "ntk_r2_group.cuh"
+#include "ntk_r2_tma.cuh"
 
 namespace ntk {
 namespace r2 {
 
-constexpr unsigned FULL = 0xffffffffu;
-constexpr unsigned STATUS_TIMEOUT = 2u;
-constexpr unsigned RANGE_MAG = 1151u << 20;  // high word of 2^128
-
-// ---------------------------------------------------------------------------
-// mbarrier / TMA (cp.async.bulk.tensor) helpers
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-// Bounded wait for phase `parity` of the barrier: false when it did not
-// complete within the limit (then the caller raises STATUS_TIMEOUT).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-  for (int it = 0; it < (1 << 22); ++it) {
-    unsigned ok;
-    asm volatile(
-        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
-}
-__device__ __forceinline__ void tma_load(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
-                                         uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-      "[%6];" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
-      : "memory");
-}
-// Fetch a box into L2 only (no shared-memory destination, no completion to
-// wait for): the load that follows finds the box in L2.
-__device__ __forceinline__ void tma_prefetch_l2(const CUtensorMap* map, int c0, int c1, int c2, int c3) {
-  asm volatile("cp.async.bulk.prefetch.tensor.4d.L2.global [%0, {%1, %2, %3, %4}];" ::"l"(map), "r"(c0), "r"(c1),
-               "r"(c2), "r"(c3)
-               : "memory");
-}
-__device__ __forceinline__ void tma_store(const CUtensorMap* map, int c0, int c1, int c2, int c3, const void* src) {
-  asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%1, %2, %3, %4}], [%5];" ::"l"(map),
-               "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(src))
-               : "memory");
-}
-__device__ __forceinline__ void tma_store_commit_and_wait() {
-  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ unsigned char* align1024(unsigned char* p) {
-  return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 1023) & ~(uintptr_t)1023);
-}
-
-// Barriers over the threads that work on one group: the whole CTA, or a
-// named barrier (id 1..15) over `count` threads of it.  all(v): a barrier
-// that also returns whether v holds in every participating thread.
-struct SyncAll {
-  __device__ __forceinline__ void operator()() const { __syncthreads(); }
-  __device__ __forceinline__ bool all(bool v) const { return __syncthreads_and(v) != 0; }
-};
-struct SyncBar {
-  int id, count;
-  __device__ __forceinline__ void operator()() const {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-  }
-  __device__ __forceinline__ bool all(bool v) const {
-    unsigned r;
-    asm volatile(
-        "{ .reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.and.pred q, %2, %3, p; selp.u32 %0, 1, 0, q; }"
-        : "=r"(r)
-        : "r"((unsigned)v), "r"(id), "r"(count)
-        : "memory");
-    return r != 0;
-  }
-};
-
 // ---------------------------------------------------------------------------
 // contiguous systems
 // ---------------------------------------------------------------------------
-// Offset (in doubles) of rows 2i, 2i+1 of chunk j in a 4 KB system tile
-// written by TMA with the 128-byte swizzle: 16-byte unit i XOR (j mod 8).
-__device__ __forceinline__ int xpair(int j, int i) { return j * 16 + ((i ^ (j & 7)) << 1); }
-
 // S contiguous systems (one warp each) solved in place in their swizzled
 // tile by the S * 32 threads gt = 0 .. of a group: TMA load of the box at
 // coordinates (0, 0, c2, c3) of tin, solve, TMA store to tout.
@@ -218,92 +130,10 @@ __device__ __forceinline__ void contiguous_group(double* tile, float2* bnd, uint
       }
     }
   }
-  // ---- FP32 solve ----
-  {
-    float CA = __shfl_up_sync(FULL, fwd_local(v, K), 1);
-    if (j == 0) CA = 0.f;
-    bwd_local(v, CA, K);
-    float XB = __shfl_down_sync(FULL, start_comb(v, K), 1);
-    if (j == 31) XB = 0.f;
-    bwd_fix(v, XB, K);
-    if (j == 0) head_fix(v, K);
-    if (j == 31) tail_fix(v, K);
-  }
-  if (SWEEPS == 0) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      double oa0, ob0, oa1, ob1;
-      out_pair0(v[2 * i], a, oa0, ob0);
-      out_pair0(v[2 * i + 1], a, oa1, ob1);
-      *reinterpret_cast<double2*>(sy + xpair(j, i)) = make_double2(oa0, oa1);
-      *reinterpret_cast<double2*>(sy + xpair(j, i + 4)) = make_double2(ob0, ob1);
-    }
-  } else {
-    // ---- residual ----
-    float xl = __shfl_up_sync(FULL, v[7].y, 1);
-    float xr = __shfl_down_sync(FULL, v[0].x, 1);
-    if (j == 0) xl = 0.f;
-    if (j == 31) xr = 0.f;
-    // the special rows' residuals (patched in after the interior ones)
-    float rsp[2] = {0.f, 0.f};
-    if (j == 0) {
-#pragma unroll
-      for (int q = 0; q < 2; ++q)
-        if (q < a.nh) {
-          const float2 d = reinterpret_cast<const float2*>(sy + xpair(0, 0))[q];
-          rsp[q] = res_row(d.x, d.y, q == 0 ? 0.f : v[q - 1].x, v[q].x, v[q + 1].x, a.hd[q][0], a.hd[q][1],
-                           a.hd[q][2]);
-        }
-    }
-    if (j == 31) {
-#pragma unroll
-      for (int q = 0; q < 2; ++q)
-        if (q < a.nt) {
-          const int k = 7 - q;  // row n-1-q is B[k] of the last chunk
-          const float2 d = reinterpret_cast<const float2*>(sy + xpair(31, (8 + k) >> 1))[(8 + k) & 1];
-          const int ti = a.nt - 1 - q;
-          rsp[q] = res_row(d.x, d.y, v[k - 1].y, v[k].y, q == 0 ? 0.f : v[k + 1].y, a.td[ti][0], a.td[ti][1],
-                           a.td[ti][2]);
-        }
-    }
-    float2 r[8];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float4 qa = *reinterpret_cast<const float4*>(sy + xpair(j, i));
-      const float4 qb = *reinterpret_cast<const float4*>(sy + xpair(j, i + 4));
-      const int k0 = 2 * i, k1 = 2 * i + 1;
-      const float2 xm0 = (k0 == 0) ? pair(xl, v[7].x) : v[k0 - 1];
-      r[k0] = res_pair(pair(qa.x, qb.x), pair(qa.y, qb.y), xm0, v[k0], v[k0 + 1], a);
-      const float2 xp1 = (k1 == 7) ? pair(v[0].y, xr) : v[k1 + 1];
-      r[k1] = res_pair(pair(qa.z, qb.z), pair(qa.w, qb.w), v[k1 - 1], v[k1], xp1, a);
-    }
-    if (j == 0) {
-      if (a.nh > 0) r[0].x = rsp[0];
-      if (a.nh > 1) r[1].x = rsp[1];
-    }
-    if (j == 31) {
-      if (a.nt > 0) r[7].y = rsp[0];
-      if (a.nt > 1) r[6].y = rsp[1];
-    }
-    // ---- FP32 correction solve ----
-    float CA = __shfl_up_sync(FULL, fwd_local(r, K), 1);
-    if (j == 0) CA = 0.f;
-    bwd_local(r, CA, K);
-    float XB = __shfl_down_sync(FULL, start_comb(r, K), 1);
-    if (j == 31) XB = 0.f;
-    bwd_fix(r, XB, K);
-    if (j == 0) head_fix(r, K);
-    if (j == 31) tail_fix(r, K);
-    // ---- s (x + delta) as FP64, in place ----
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      double oa0, ob0, oa1, ob1;
-      out_pair(v[2 * i], r[2 * i], a, oa0, ob0);
-      out_pair(v[2 * i + 1], r[2 * i + 1], a, oa1, ob1);
-      *reinterpret_cast<double2*>(sy + xpair(j, i)) = make_double2(oa0, oa1);
-      *reinterpret_cast<double2*>(sy + xpair(j, i + 4)) = make_double2(ob0, ob1);
-    }
-  }
+  contiguous_solve<SWEEPS>(v, sy, j, a, [&](int i, double oa0, double oa1, double ob0, double ob1) {
+    *reinterpret_cast<double2*>(sy + xpair(j, i)) = make_double2(oa0, oa1);
+    *reinterpret_cast<double2*>(sy + xpair(j, i + 4)) = make_double2(ob0, ob1);
+  });
   if (__any_sync(FULL, rmax >= RANGE_MAG) && j == 0 && a.status) atomicOr(a.status, 1u);
   fence_proxy_async();
   sync();
@@ -331,9 +161,6 @@ __global__ void __launch_bounds__(512, 2)
 // ---------------------------------------------------------------------------
 // strided systems
 // ---------------------------------------------------------------------------
-constexpr int SG = 16;  // systems per group (128 contiguous bytes per row)
-// exchange arrays, [chunk][system] floats each
-enum { X_E1 = 0, X_S1, X_A0, X_B0, X_B7, X_E2, X_S2, X_COUNT };
 constexpr size_t S_TILE_BYTES = (size_t)NROWS * SG * 8;
 constexpr size_t S_XCH_FLOATS = (size_t)X_COUNT * CHUNKS * SG;
 constexpr size_t S_SMEM = 1024 + S_TILE_BYTES + S_XCH_FLOATS * 4 + 16;
@@ -417,100 +244,19 @@ __device__ __forceinline__ unsigned strided_group(double* tile, float* xch, int 
       else v[k - HALF].y = h;
     }
   }
-  // ---- FP32 solve ----
-  X(X_E1, c) = fwd_local(v, K);
-  sync();  // carries published; every halo row has been read
-  if (RHS == RHS_COMPACT && SWEEPS > 0) {
-    reinterpret_cast<float2*>(col + r0 * SG)[0] = edge0;
-    reinterpret_cast<float2*>(col + (r0 + ROWS - 1) * SG)[0] = edge15;
-  }
-  bwd_local(v, c > 0 ? X(X_E1, c - 1) : 0.f, K);
-  const float S1 = start_comb(v, K);
-  X(X_S1, c) = S1;
-  X(X_A0, c) = v[0].x;
-  X(X_B0, c) = v[0].y;
-  X(X_B7, c) = v[7].y;
-  sync();
-  bwd_fix(v, c < CHUNKS - 1 ? X(X_S1, c + 1) : 0.f, K);
-  if (c == 0) head_fix(v, K);
-  if (c == CHUNKS - 1) tail_fix(v, K);
-  if (SWEEPS == 0) {
-    double* out = DIRECT ? out_of() : col + r0 * SG;
-    const long long step = DIRECT ? es : SG;
-    if (out) {
-#pragma unroll
-      for (int k = 0; k < HALF; ++k) {
-        double oa, ob;
-        out_pair0(v[k], a, oa, ob);
-        out[k * step] = oa;
-        out[(k + HALF) * step] = ob;
-      }
-    }
-    return rmax;
-  }
-  // ---- residual ----
-  const float xl = c > 0 ? left_edge(X(X_B7, c - 1), S1, K) : 0.f;
-  const float xr =
-      c < CHUNKS - 1 ? right_edge(X(X_A0, c + 1), X(X_B0, c + 1), c + 2 < CHUNKS ? X(X_S1, c + 2) : 0.f, K) : 0.f;
-  // the special rows' residuals (patched in after the interior ones)
-  float rsp[2] = {0.f, 0.f};
-  if (c == 0) {
-#pragma unroll
-    for (int q = 0; q < 2; ++q)
-      if (q < a.nh) {
-        const float2 d = reinterpret_cast<const float2*>(col + q * SG)[0];
-        rsp[q] =
-            res_row(d.x, d.y, q == 0 ? 0.f : v[q - 1].x, v[q].x, v[q + 1].x, a.hd[q][0], a.hd[q][1], a.hd[q][2]);
-      }
-  }
-  if (c == CHUNKS - 1) {
-#pragma unroll
-    for (int q = 0; q < 2; ++q)
-      if (q < a.nt) {
-        const int k = HALF - 1 - q;
-        const float2 d = reinterpret_cast<const float2*>(col + (r0 + HALF + k) * SG)[0];
-        const int ti = a.nt - 1 - q;
-        rsp[q] = res_row(d.x, d.y, v[k - 1].y, v[k].y, q == 0 ? 0.f : v[k + 1].y, a.td[ti][0], a.td[ti][1],
-                         a.td[ti][2]);
-      }
-  }
-  float2 r[8];
-#pragma unroll
-  for (int k = 0; k < HALF; ++k) {
-    const float2 da = reinterpret_cast<const float2*>(col + (r0 + k) * SG)[0];
-    const float2 db = reinterpret_cast<const float2*>(col + (r0 + k + HALF) * SG)[0];
-    const float2 xm = (k == 0) ? pair(xl, v[HALF - 1].x) : v[k - 1];
-    const float2 xp = (k == HALF - 1) ? pair(v[0].y, xr) : v[k + 1];
-    r[k] = res_pair(pair(da.x, db.x), pair(da.y, db.y), xm, v[k], xp, a);
-  }
-  if (c == 0) {
-    if (a.nh > 0) r[0].x = rsp[0];
-    if (a.nh > 1) r[1].x = rsp[1];
-  }
-  if (c == CHUNKS - 1) {
-    if (a.nt > 0) r[HALF - 1].y = rsp[0];
-    if (a.nt > 1) r[HALF - 2].y = rsp[1];
-  }
-  // ---- FP32 correction solve ----
-  X(X_E2, c) = fwd_local(r, K);
-  sync();
-  bwd_local(r, c > 0 ? X(X_E2, c - 1) : 0.f, K);
-  X(X_S2, c) = start_comb(r, K);
-  sync();
-  bwd_fix(r, c < CHUNKS - 1 ? X(X_S2, c + 1) : 0.f, K);
-  if (c == 0) head_fix(r, K);
-  if (c == CHUNKS - 1) tail_fix(r, K);
-  double* out = DIRECT ? out_of() : col + r0 * SG;
-  const long long step = DIRECT ? es : SG;
-  if (out) {
-#pragma unroll
-    for (int k = 0; k < HALF; ++k) {
-      double oa, ob;
-      out_pair(v[k], r[k], a, oa, ob);
-      out[k * step] = oa;
-      out[(k + HALF) * step] = ob;
-    }
-  }
+  strided_solve<SWEEPS, SG>(
+      v, col, xch, s, c, a, sync,
+      [&] {
+        if (RHS == RHS_COMPACT && SWEEPS > 0) {
+          reinterpret_cast<float2*>(col + r0 * SG)[0] = edge0;
+          reinterpret_cast<float2*>(col + (r0 + ROWS - 1) * SG)[0] = edge15;
+        }
+      },
+      [&](int k, double val) {
+        double* out = DIRECT ? out_of() : col + r0 * SG;
+        const long long step = DIRECT ? es : SG;
+        if (out) out[k * step] = val;
+      });
   return rmax;
 }
 
@@ -740,45 +486,6 @@ __global__ void __launch_bounds__(1024, 1)
 // host side
 // ---------------------------------------------------------------------------
 namespace {
-
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  });
-  return fn;
-}
-
-bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
-
-// Rank-4 map (unused trailing dimensions of extent 1) over `base`.
-int encode(CUtensorMap* m, const double* base, const cuuint64_t dims[4], const cuuint64_t strides[3],
-           const cuuint32_t box[4], CUtensorMapSwizzle sw) {
-  EncodeTiledFn fn = encode_fn();
-  if (!fn) {
-    set_error("cuTensorMapEncodeTiled is not available from the driver");
-    return NTK_ERR_UNSUPPORTED;
-  }
-  const cuuint32_t es[4] = {1, 1, 1, 1};
-  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<double*>(base), dims, strides, box, es,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) {
-    set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
-    return NTK_ERR_UNSUPPORTED;
-  }
-  return NTK_OK;
-}
 
 template <int RHS, int SWEEPS>
 int launch_x(const double* in, double* out, const Batch& b, const Args& a, int S, cudaStream_t st) {
