@@ -383,7 +383,7 @@ int half_step(AdiRefine* ar, const double* in, double* out, long long is, long l
 }  // namespace
 
 int adi_refine_step(AdiRefine* ar, double* u, double* d_x, const double* d_y, cudaStream_t st) {
-  if (ar->r2a) return r2::adi_step(ar->r2a, u, d_x, d_y, ar->wx, st);
+  if (ar->r2a) return r2::adi_step(ar->r2a, u, d_x, d_y, st);
   const int N = ar->N;
   // x half: systems = rows 1..N-2, stencil of u's rows, boundary RHS from d_x
   int rc = half_step(ar, u + N, d_x + N, N, 1, d_x + N, N, 1, ar->wx, st);

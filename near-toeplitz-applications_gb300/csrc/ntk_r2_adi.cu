@@ -13,17 +13,17 @@
 //
 //  * x half step (r2ax_kernel): the systems are rows 1..N-2 of the field;
 //    a CTA solves S consecutive rows of one window.  One TMA box brings the
-//    S + 2 rows of u its stencils read (512 columns each, 128-byte swizzle),
-//    the (hi, lo) RHS pairs go to a second shared array (the stencil rows
-//    are shared between systems), and each thread stores the window's
-//    central rows of its chunk straight to d_x.
+//    S + 2 rows of u its stencils read (512 columns each, 128-byte swizzle);
+//    once every stencil has been formed (a CTA barrier, the pairs held in
+//    registers across it) each system's (hi, lo) RHS pairs overwrite its
+//    middle row, and each thread stores the window's central rows of its
+//    chunk straight to d_x.
 //  * y half step (r2ay_kernel): the systems are columns 1..N-2 of d_x; a CTA
 //    solves 16 adjacent columns of one window from an [512][18] tile (the
-//    16 columns and their two neighbours, two TMA boxes).  A thread's
-//    stencil neighbours are its neighbour lanes' own values (shuffles), so
-//    every thread rewrites its own column in place with the (hi, lo) pairs;
-//    the central rows go straight into u's columns, where the reference's
-//    final transpose puts them.
+//    16 columns and their two neighbours, two TMA boxes).  After a CTA
+//    barrier every thread rewrites its own column in place with the (hi, lo)
+//    pairs; the central rows go straight into u's columns, where the
+//    reference's final transpose puts them.
 #include <cmath>
 
 #include "ntk_r2_adi.h"
@@ -64,16 +64,18 @@ __device__ __forceinline__ double stencil(double lo, double mid, double hi, doub
   return GZ ? t : dfma_(gamma, mid, t);
 }
 
-// ---- x half step: S rows of the field per CTA, one window ----
+// ---- x half step: S = 4 rows of the field per CTA, one window ----
+// Seven 4-warp CTAs per SM (72 registers: the RHS pairs are held across the
+// barrier that frees the stencil rows).
+constexpr int AX_S = 4;
 template <int SWEEPS, bool GZ>
-__global__ void __launch_bounds__(512, 2)
+__global__ void __launch_bounds__(32 * AX_S, 7)
     r2ax_kernel(const __grid_constant__ CUtensorMap tu, double* out, const __grid_constant__ AdiWin g,
                 const __grid_constant__ AdiKinds ak) {
   extern __shared__ unsigned char smem_raw[];
-  const int S = blockDim.x >> 5;
+  constexpr int S = AX_S;
   double* tile = reinterpret_cast<double*>(align1024(smem_raw));  // [S + 2][512] stencil rows
-  double* hlb = tile + (size_t)(S + 2) * NROWS;                    // [S][512] (hi, lo) pairs
-  uint64_t* bar = reinterpret_cast<uint64_t*>(hlb + (size_t)S * NROWS);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tile + (size_t)(S + 2) * NROWS);
   const int nblk = (g.ns + S - 1) / S;
   const int w = blockIdx.x / nblk;
   const int s0 = (blockIdx.x - w * nblk) * S;
@@ -92,33 +94,46 @@ __global__ void __launch_bounds__(512, 2)
     return;
   }
   const int s = s0 + warp;  // system s: row s + 1 of the field
-  if (s >= g.ns) return;    // no CTA barrier follows
+  const bool live = s < g.ns;
   const double* rlo = tile + (size_t)warp * NROWS;
-  const double* rmid = rlo + NROWS;
-  const double* rhi = rmid + NROWS;
-  double* hl = hlb + (size_t)warp * NROWS;
+  double* hl = tile + (size_t)(warp + 1) * NROWS;  // the middle row, rewritten with the pairs
+  const double* rhi = hl + NROWS;
   unsigned rmax = 0;
-  float2 v[8];
+  float2 v[8], lo8[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const double2 ql = *reinterpret_cast<const double2*>(rlo + xpair(j, i));
-    const double2 qm = *reinterpret_cast<const double2*>(rmid + xpair(j, i));
+    const double2 qm = *reinterpret_cast<const double2*>(hl + xpair(j, i));
     const double2 qh = *reinterpret_cast<const double2*>(rhi + xpair(j, i));
     double d0 = stencil<GZ>(ql.x, qm.x, qh.x, g.gamma);
     double d1 = stencil<GZ>(ql.y, qm.y, qh.y, g.gamma);
     // identity rows take the boundary values (experiments/run-adi.py:50-53)
-    if (i == 0 && j == 0 && (kind == 0 || kind == 3)) d0 = g.bnd[(long long)s * g.N];
-    if (i == 7 && j == 31 && (kind == 2 || kind == 3)) d1 = g.bnd[(long long)s * g.N + g.N - 1];
+    if (live && i == 0 && j == 0 && (kind == 0 || kind == 3)) d0 = g.bnd[(long long)s * g.N];
+    if (live && i == 7 && j == 31 && (kind == 2 || kind == 3)) d1 = g.bnd[(long long)s * g.N + g.N - 1];
     float h0, l0, h1, l1;
     split_f64(d0, h0, l0, rmax);
     split_f64(d1, h1, l1, rmax);
-    if (SWEEPS > 0) *reinterpret_cast<float4*>(hl + xpair(j, i)) = make_float4(h0, l0, h1, l1);
     if (i < 4) {
       v[2 * i].x = h0;
       v[2 * i + 1].x = h1;
+      lo8[2 * i].x = l0;
+      lo8[2 * i + 1].x = l1;
     } else {
       v[2 * i - 8].y = h0;
       v[2 * i - 7].y = h1;
+      lo8[2 * i - 8].y = l0;
+      lo8[2 * i - 7].y = l1;
+    }
+  }
+  __syncthreads();  // every stencil row has been read
+  if (!live) return;  // no CTA barrier follows
+  if (SWEEPS > 0) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      *reinterpret_cast<float4*>(hl + xpair(j, i)) =
+          make_float4(v[2 * i].x, lo8[2 * i].x, v[2 * i + 1].x, lo8[2 * i + 1].x);
+      *reinterpret_cast<float4*>(hl + xpair(j, i + 4)) =
+          make_float4(v[2 * i].y, lo8[2 * i].y, v[2 * i + 1].y, lo8[2 * i + 1].y);
     }
   }
   double* dst = out + (long long)s * g.N + start + ROWS * j;  // row 16 j of the window
@@ -167,25 +182,32 @@ __global__ void __launch_bounds__(512, 2)
   double* col = tile + 1 + s;  // own column, row r at col[r * YP]
   const int r0 = ROWS * c;
   unsigned rmax = 0;
-  float2 v[8];
+  float2 v[8], lo8[8];
 #pragma unroll
   for (int k = 0; k < ROWS; ++k) {
     const int r = r0 + k;
-    const double m = col[r * YP];
-    double dl = __shfl_up_sync(FULL, m, 1, 16);
-    double dh = __shfl_down_sync(FULL, m, 1, 16);
-    if (s == 0) dl = tile[r * YP];
-    if (s == SG - 1) dh = tile[r * YP + YP - 1];
-    double d = stencil<GZ>(dl, m, dh, g.gamma);
+    const double d0 = col[r * YP - 1], m = col[r * YP], d2 = col[r * YP + 1];
+    double d = stencil<GZ>(d0, m, d2, g.gamma);
     if (k == 0 && c == 0 && (kind == 0 || kind == 3)) d = live ? g.bnd[(long long)sys * g.N] : 0.0;
     if (k == ROWS - 1 && c == CHUNKS - 1 && (kind == 2 || kind == 3))
       d = live ? g.bnd[(long long)sys * g.N + g.N - 1] : 0.0;
     float h, l;
     split_f64(d, h, l, rmax);
-    // only this thread reads its own column from the tile: rewrite in place
-    if (SWEEPS > 0) reinterpret_cast<float2*>(col + r * YP)[0] = make_float2(h, l);
-    if (k < HALF) v[k].x = h;
-    else v[k - HALF].y = h;
+    if (k < HALF) {
+      v[k].x = h;
+      lo8[k].x = l;
+    } else {
+      v[k - HALF].y = h;
+      lo8[k - HALF].y = l;
+    }
+  }
+  __syncthreads();  // every stencil column has been read
+  if (SWEEPS > 0) {
+#pragma unroll
+    for (int k = 0; k < HALF; ++k) {
+      reinterpret_cast<float2*>(col + (r0 + k) * YP)[0] = make_float2(v[k].x, lo8[k].x);
+      reinterpret_cast<float2*>(col + (r0 + k + HALF) * YP)[0] = make_float2(v[k].y, lo8[k].y);
+    }
   }
   double* dst = out + (long long)(start + r0) * g.N + sys;  // row r0 of column sys + 1 of u
   strided_solve<SWEEPS, YP>(v, col, xch, s, c, a, SyncAll(), [] {}, [&](int k, double val) {
@@ -279,13 +301,13 @@ int launch_kernel(K kern, unsigned grid, unsigned block, size_t smem, cudaStream
 
 }  // namespace
 
-int adi_step(AdiR2* r, double* u, double* d_x, const double* d_y, int wx, cudaStream_t st) {
+int adi_step(AdiR2* r, double* u, double* d_x, const double* d_y, cudaStream_t st) {
   if (!aligned16(u) || !aligned16(d_x)) {
     set_error("ADI: u and d_x must be 16-byte aligned");
     return NTK_ERR_INVALID;
   }
   const int N = r->geo.N;
-  const int S = (wx == 8) ? 8 : 4;
+  constexpr int S = AX_S;
   const cuuint64_t n = (cuuint64_t)N;
   // x half step: u as (column in chunk, chunk, row), box of S + 2 rows
   CUtensorMap mu, md;
@@ -307,7 +329,7 @@ int adi_step(AdiR2* r, double* u, double* d_x, const double* d_y, int wx, cudaSt
   gx.bnd = d_x + N;  // system s, row i: d_x[(s + 1) N + i]
   gy.bnd = d_y + N;  // system s, row i: d_y[(s + 1) N + i]
   const int P = r->geo.whole ? 1 : r->geo.P;
-  const size_t xsmem = 1024 + (size_t)(2 * S + 2) * NROWS * 8 + 16;
+  const size_t xsmem = 1024 + (size_t)(S + 2) * NROWS * 8 + 16;
   const unsigned xgrid = (unsigned)(P * ((r->geo.ns + S - 1) / S));
   const unsigned ygrid = (unsigned)(P * ((r->geo.ns + SG - 1) / SG));
   int rc;

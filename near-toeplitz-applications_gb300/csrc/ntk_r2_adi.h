@@ -23,8 +23,7 @@ void adi_destroy(AdiR2* r);
 // One ADI step (experiments/run-adi.py:59-71): x half step from u into
 // d_x (rows 1..N-2, boundary RHS d_x's own boundary columns), y half step
 // from d_x into u's columns 1..N-2 (boundary RHS d_y's boundary columns).
-// wx: systems per CTA of the x half step (4 or 8).
-int adi_step(AdiR2* r, double* u, double* d_x, const double* d_y, int wx, cudaStream_t st);
+int adi_step(AdiR2* r, double* u, double* d_x, const double* d_y, cudaStream_t st);
 void adi_status_words(const AdiR2* r, std::vector<unsigned*>& out);
 
 }  // namespace r2
