@@ -686,7 +686,7 @@ def secondary_configs(dev, hbm):
     for prec in worst:
         ub[prec]["rel_err_vs_banded_oracle_128_systems"] = worst[prec]
     ub.update({"workload": "4096 systems, lengths log-uniform in [32, 8192], 512-row windows, one warp each "
-                           "(FP64: one launch; FP32 + refine: full and padded windows)", "rows": total_rows,
+                           "(one launch per solve in both precisions)", "rows": total_rows,
                "speedup_refine_vs_fp64": ub["fp64"]["ms"] / ub["fp32_refine"]["ms"],
                "cpu_baseline": {"rows_per_s": cpu_rows / cpu_s, "cores": 1, "kind": "port",
                                 "sample": "128 systems, one scipy solve_banded each"}})

@@ -60,6 +60,10 @@ struct F64Win {
   int n, w0, lo, hi;
   int head, Kh, tail, pad_;
   double cl, cg, cw;
+  // central rows r < blo or r >= bhi are border rows (a neighbouring window
+  // reads them): written to work during the solve, copied into d at the end
+  int blo, bhi;
+  int sysi, wfirst, wcount;  // the system's counter and windows
 };
 
 namespace {
@@ -162,25 +166,19 @@ __device__ __forceinline__ void f64w_fac(const F64Win& w, const double* __restri
   if (r == F64W_LW - 1 && i < w.n - 1) c = 0.0;  // cut end
 }
 
-__global__ void __launch_bounds__(128, 5) batch_f64w_kernel(const double* __restrict__ work, double* __restrict__ d,
-                                                            const F64Win* __restrict__ wins, long long nwin,
-                                                            const double* __restrict__ pool) {
-  __shared__ __align__(16) double tiles[F64W_WARPS * F64W_PITCH];
+// Window wi by one warp: all rows read from d, the central rows written to d
+// except the border rows, which go to work.
+__device__ __forceinline__ void f64_window(double* work, double* d, const F64Win* __restrict__ wins,
+                                        long long wi, const double* __restrict__ pool, double* tile, int lane) {
   constexpr int M = F64W_M;
   constexpr unsigned FULL = 0xffffffffu;
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  const long long wi = (long long)blockIdx.x * F64W_WARPS + warp;
-  if (wi >= nwin) return;  // whole warps leave; no CTA barrier follows
   const F64Win w = wins[wi];
-  double* tile = tiles + warp * F64W_PITCH;
-  const double* src = work + w.off + w.w0;
   // stage rows (coalesced); padding rows are zero-filled
 #pragma unroll
   for (int q = 0; q < M; ++q) {
     const int r = lane + 32 * q;
     const bool ok = w.w0 + r < w.n;
-    cp_async8(tile + (r / M) * (M + 1) + (r % M), ok ? src + r : work, ok ? 8u : 0u);
+    cp_async8(tile + (r / M) * (M + 1) + (r % M), ok ? d + w.off + w.w0 + r : d, ok ? 8u : 0u);
   }
   cp_async_wait_all();
   __syncwarp();
@@ -259,12 +257,63 @@ __global__ void __launch_bounds__(128, 5) batch_f64w_kernel(const double* __rest
 #pragma unroll
   for (int k = 0; k < M; ++k) tile[lane * (M + 1) + k] = v[k];
   __syncwarp();
-  double* dst = d + w.off + w.w0;
+  const long long base = w.off + w.w0;
+  const int blo = __ldg(&wins[wi].blo), bhi = __ldg(&wins[wi].bhi);  // loaded late: not live across the solve
 #pragma unroll
   for (int q = 0; q < M; ++q) {
     const int r = lane + 32 * q;
-    if (r >= w.lo && r < w.hi) dst[r] = tile[(r / M) * (M + 1) + (r % M)];
+    if (r >= w.lo && r < w.hi) (r < blo || r >= bhi ? work : d)[base + r] = tile[(r / M) * (M + 1) + (r % M)];
   }
+}
+
+// All windows in one launch, in place, without a copy of the whole buffer
+// and without waiting: every window reads its rows from d and writes its
+// central rows to d except its border rows (central rows a neighbouring
+// window reads), which go to work, so d keeps every halo row unchanged while
+// the system's windows run; each window of a multi-window system then counts
+// itself done on the system's counter, and the window that finishes last
+// copies the system's border rows from work into d and resets the counter.
+// Each warp first prefetches into L2 the window of the warp pf CTAs further
+// on (pf = the CTAs resident at once), so that window's staging finds it in
+// L2.
+__global__ void __launch_bounds__(128, 5) batch_f64w_kernel(double* work, double* d, const F64Win* __restrict__ wins,
+                                                            long long nwin, const double* __restrict__ pool,
+                                                            unsigned* done, unsigned pf) {
+  __shared__ __align__(16) double tiles[F64W_WARPS * F64W_PITCH];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long wi = (long long)blockIdx.x * F64W_WARPS + warp;
+  const long long wp = wi + (long long)pf * F64W_WARPS;
+  if (lane == 0 && pf > 0 && wp < nwin) {
+    const long long base = __ldg(&wins[wp].off) + __ldg(&wins[wp].w0);
+    const int rows = min(F64W_LW, __ldg(&wins[wp].n) - __ldg(&wins[wp].w0));
+    const uintptr_t a = reinterpret_cast<uintptr_t>(d + base) & ~(uintptr_t)15;
+    const uintptr_t e = (reinterpret_cast<uintptr_t>(d + base + rows) + 15) & ~(uintptr_t)15;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)(e - a)) : "memory");
+  }
+  if (wi >= nwin) return;  // whole warps leave; no CTA barrier follows
+  f64_window(work, d, wins, wi, pool, tiles + warp * F64W_PITCH, lane);
+  const int wcount = __ldg(&wins[wi].wcount);
+  if (wcount < 2) return;
+  __syncwarp();
+  unsigned last = 0;
+  const int sysi = __ldg(&wins[wi].sysi);
+  if (lane == 0) {
+    __threadfence();
+    last = atomicAdd(done + sysi, 1u) == (unsigned)wcount - 1;
+    if (last) __threadfence();
+  }
+  if (!__shfl_sync(0xffffffffu, last, 0)) return;
+  border_copy(work, d, __ldg(&wins[wi].wfirst), wcount, (unsigned)lane,
+              [&](int g, long long& base, int& lo, int& blo, int& bhi, int& hi) {
+                const F64Win* v = wins + g;
+                base = __ldg(&v->off) + __ldg(&v->w0);
+                lo = __ldg(&v->lo);
+                hi = __ldg(&v->hi);
+                blo = min(__ldg(&v->blo), hi);
+                bhi = max(__ldg(&v->bhi), lo);
+              });
+  if (lane == 0) done[sysi] = 0u;
 }
 
 }  // namespace
@@ -286,9 +335,13 @@ struct Batch_ {
   F64Win* d_wins = nullptr;       // NTK_FP64 windows (batch_f64w_kernel); null: batch_f64_kernel
   long long nwin = 0;
 
+  unsigned* d_done = nullptr;      // per system: its windows finished in the current launch
+  unsigned wpf = 0;                // the window kernel's prefetch distance (CTAs resident at once)
+
   ~Batch_() {
     if (refine) batch_refine_destroy(refine);
     if (d_wins) cudaFree(d_wins);
+    if (d_done) cudaFree(d_done);
     if (d_desc) cudaFree(d_desc);
     if (d_order) cudaFree(d_order);
     if (d_pool) cudaFree(d_pool);
@@ -433,7 +486,7 @@ bool cut_sequence(const Matrix& m, int w0, int limit, std::vector<double>& pool,
 
 // FP64 windows of one system (see batch_f64w_kernel), appended to `wins`;
 // false when the factors decay too slowly for 128 central rows per window.
-bool system_windows(int n, const double* in3, const double* h6, const double* t6, const SysDesc& sd,
+bool system_windows(int n, const double* in3, const double* h6, const double* t6, const SysDesc& sd, int sysi,
                     std::vector<double>& pool, std::vector<F64Win>& wins, int& count) {
   constexpr int LW = F64W_LW;
   F64Win base{};
@@ -444,6 +497,8 @@ bool system_windows(int n, const double* in3, const double* h6, const double* t6
   if (n <= LW) {  // one window, padded with identity rows
     F64Win w = base;
     w.w0 = 0, w.lo = 0, w.hi = n;
+    w.blo = 0, w.bhi = n;  // a whole system: no border rows
+    w.sysi = sysi, w.wfirst = (int)wins.size(), w.wcount = 1;
     w.head = sd.tab, w.Kh = sd.K;
     w.cl = sd.l_inf, w.cg = sd.g_inf, w.cw = sd.w_inf;
     wins.push_back(w);
@@ -494,6 +549,18 @@ bool system_windows(int n, const double* in3, const double* h6, const double* t6
     const int tab = (int)pool.size();
     if (!cut_sequence(m, last_w0, LW / 4, pool, Kl, cl)) return false;
     add(last_w0, pos - last_w0, LW, tab, Kl, cl);
+  }
+  // border rows: central rows the neighbouring windows read
+  const size_t first = wins.size() - count;
+  for (int g = 0; g < count; ++g) {
+    F64Win& w = wins[first + g];
+    w.sysi = sysi;
+    w.wfirst = (int)first;
+    w.wcount = count;
+    w.blo = w.lo;
+    w.bhi = w.hi;
+    if (g > 0) w.blo = std::min(w.hi, wins[first + g - 1].w0 + LW - w.w0);
+    if (g + 1 < count) w.bhi = std::max(w.lo, wins[first + g + 1].w0 - w.w0);
   }
   return true;
 }
@@ -573,7 +640,7 @@ int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long l
     bool ok = true;
     for (long long s = 0; s < nsys && ok; ++s) {
       int count = 0;
-      ok = ntk::system_windows(n[s], interior + 3 * s, head + 6 * s, tail + 6 * s, desc[s], pool, wins, count);
+      ok = ntk::system_windows(n[s], interior + 3 * s, head + 6 * s, tail + 6 * s, desc[s], (int)s, pool, wins, count);
       multi += count > 1;
     }
     if (ok) {
@@ -618,6 +685,17 @@ int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long l
     int sms = 148;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
     b->grid = sms * 8;  // 8 CTAs of 4 warps per SM, persistent
+    if (!rc && b->d_wins) {
+      int per_sm = 0;
+      rc = ntk::cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ntk::batch_f64w_kernel,
+                                                                          32 * ntk::F64W_WARPS, 0),
+                            "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+      b->wpf = (unsigned)(per_sm * sms);
+      if (!rc)
+        rc = ntk::cuda_status(cudaMalloc(&b->d_done, sizeof(unsigned) * (size_t)nsys), "cudaMalloc(system counters)");
+      if (!rc)
+        rc = ntk::cuda_status(cudaMemset(b->d_done, 0, sizeof(unsigned) * (size_t)nsys), "cudaMemset(system counters)");
+    }
     if (!rc && precision != NTK_FP64)
       rc = ntk::batch_refine_create(&b->refine, nsys, n, offset, interior, head, tail, precision);
   }
@@ -667,16 +745,12 @@ int ntk_batch_solve(ntk_batch* b, double* d, void* stream) {
     return NTK_ERR_INVALID;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  if (b->refine) return ntk::batch_refine_solve(b->refine, d, b->d_scratch, b->total, st);
+  if (b->refine) return ntk::batch_refine_solve(b->refine, d, b->d_scratch, st);
   if (b->d_wins) {
-    // windows overlap: read from a copy of d
-    int rc = ntk::cuda_status(
-        cudaMemcpyAsync(b->d_scratch, d, sizeof(double) * (size_t)b->total, cudaMemcpyDeviceToDevice, st),
-        "cudaMemcpyAsync(window input copy)");
-    if (rc) return rc;
+    // one launch: windows solved in place, border rows through work
     const long long blocks = (b->nwin + ntk::F64W_WARPS - 1) / ntk::F64W_WARPS;
     ntk::batch_f64w_kernel<<<(unsigned)blocks, 32 * ntk::F64W_WARPS, 0, st>>>(b->d_scratch, d, b->d_wins, b->nwin,
-                                                                              b->d_pool);
+                                                                              b->d_pool, b->d_done, b->wpf);
     return ntk::cuda_status(cudaGetLastError(), "batch_f64w_kernel");
   }
   int rc = ntk::cuda_status(cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), st), "cudaMemsetAsync(counter)");

@@ -13,8 +13,16 @@
 // matrices the pivots reach the fixed point within a few rows (the transient
 // shrinks by ~(a c / u^2) per row), so the tables are the window's FP32 LU;
 // they only precondition the refinement, whose residual uses the exact
-// double-word rows.  Windows overlap, so the batch copies d to its work
-// array first and the windows read from there and write d.
+// double-word rows.
+//
+// One launch, in place, no waiting: a window's halo rows (the rows it reads
+// but does not write) are the border rows of its neighbours (central rows
+// of theirs that it reads).  Every window reads its rows from d and writes
+// its central rows to d except its border rows, which go to the work array,
+// so d keeps every halo row unchanged while the system's windows run; each
+// window then counts itself done on its system's counter, and the window
+// that finishes last copies the system's border rows (about 2H per cut)
+// from work into d and resets the counter.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -37,7 +45,11 @@ struct BatchWin {
   DW td[2][3];
   DW s;                // output scale (1)
   int unit_scale = 1;
-  int pad_ = 0;
+  // central rows r < blo or r >= bhi are border rows (a neighbouring window
+  // reads them): written to work during the solve, copied into d at the end
+  int blo = 0, bhi = 0;
+  int sysi = 0;                // the system's counter
+  int wfirst = 0, wcount = 1;  // the system's windows
 };
 
 namespace refine_detail {
@@ -103,20 +115,38 @@ __device__ __forceinline__ void slot_of(const BatchWin& w, int j, int& slot, boo
   writer = (j == 1);
 }
 
+// After window w of a multi-window system: count it done; the warp of the
+// system's last window copies every border row of the system from work into
+// d (by then no window of the system reads d any more) and resets the
+// counter for the next launch.
+template <class WIN>
+__device__ __forceinline__ void finish_system(const double* work, double* d, const WIN* __restrict__ wins,
+                                              const WIN& w, unsigned* done, unsigned lane) {
+  __syncwarp();
+  unsigned last = 0;
+  if (lane == 0) {
+    __threadfence();
+    last = atomicAdd(done + w.sysi, 1u) == (unsigned)w.wcount - 1;
+    if (last) __threadfence();
+  }
+  if (!__shfl_sync(0xffffffffu, last, 0)) return;
+  border_copy(work, d, w.wfirst, w.wcount, lane, [&](int g, long long& base, int& lo, int& blo, int& bhi, int& hi) {
+    const WIN* v = wins + g;
+    base = __ldg(&v->off);
+    lo = __ldg(&v->out_lo);
+    hi = __ldg(&v->out_hi);
+    blo = min(__ldg(&v->blo), hi);
+    bhi = max(__ldg(&v->bhi), lo);
+  });
+  if (lane == 0) done[w.sysi] = 0u;
+}
+
+// Window `item` by one warp: all rows read from d, the central rows written
+// to d except the border rows, which go to work.
 template <int SWEEPS, bool PAD>
-__global__ void __launch_bounds__(32 * BW, 6) batch_refine_kernel(const double* __restrict__ src, double* dst,
-                                                               const BatchWin* __restrict__ wins, int nwins,
-                                                               unsigned* status) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int P = sys_pitch<BM>();
-  const int warp = threadIdx.x >> 5;
-  const unsigned lane = threadIdx.x & 31;
-  float4* tq = reinterpret_cast<float4*>(smem_raw) + (size_t)warp * BTAB;
-  BatchWin* wa = reinterpret_cast<BatchWin*>(reinterpret_cast<float4*>(smem_raw) + (size_t)BW * BTAB) + warp;
-  double* trow = reinterpret_cast<double*>(reinterpret_cast<BatchWin*>(reinterpret_cast<float4*>(smem_raw) +
-                                                                        (size_t)BW * BTAB) + BW) + (size_t)warp * P;
-  const long long item = (long long)blockIdx.x * BW + warp;
-  if (item >= nwins) return;  // whole warp; no CTA barriers below
+__device__ __forceinline__ void refine_window(double* work, double* dst, const BatchWin* __restrict__ wins,
+                                           long long item, unsigned* status, unsigned* done, float4* tq,
+                                           BatchWin* wa, double* trow, unsigned lane) {
   unsigned range = 0;
 
   // window descriptor into shared memory
@@ -130,12 +160,11 @@ __global__ void __launch_bounds__(32 * BW, 6) batch_refine_kernel(const double* 
   const BatchWin& w = *wa;
   // stage the window (rows lane + 32q; zero beyond nwin)
   {
-    const double* gsrc = src + w.off;
 #pragma unroll
     for (int q = 0; q < BM; ++q) {
       const int r = (int)lane + 32 * q;
       const bool ok = !PAD || r < w.nwin;
-      cp_async8(trow + tile_off<BM>(r), ok ? gsrc + r : src, ok ? 8u : 0u);
+      cp_async8(trow + tile_off<BM>(r), ok ? dst + w.off + r : dst, ok ? 8u : 0u);
     }
   }
   // FP32 factor tables of this lane's 16 rows (layout of ChunkTabs)
@@ -209,31 +238,72 @@ __global__ void __launch_bounds__(32 * BW, 6) batch_refine_kernel(const double* 
   refine_system<BM, RHS_IDENTITY, SWEEPS, false, PAD, false, BatchWin>(trow, nullptr, tabs, w.nwin, w, lane, range);
   __syncwarp();
   {
-    double* gdst = dst + w.off;
 #pragma unroll 4
     for (int q = 0; q < BM; ++q) {
       const int r = (int)lane + 32 * q;
-      if (r >= w.out_lo && r < w.out_hi) gdst[r] = trow[tile_off<BM>(r)];
+      if (r >= w.out_lo && r < w.out_hi) {
+        const bool border = r < w.blo || r >= w.bhi;
+        (border ? work : dst)[w.off + r] = trow[tile_off<BM>(r)];
+      }
     }
   }
   if (range && status) atomicOr(status, 1u);
+  if (w.wcount > 1) finish_system(work, dst, wins, w, done, lane);
+}
+
+// The padded windows' solve as a separate (not inlined) function: one
+// kernel holding both window kinds inline spills heavily; the full windows,
+// most of the rows, stay inline.
+template <int SWEEPS>
+__device__ __noinline__ void refine_window_padded(double* work, double* dst, const BatchWin* __restrict__ wins,
+                                                  long long item, unsigned* status, unsigned* done, float4* tq,
+                                                  BatchWin* wa, double* trow, unsigned lane) {
+  refine_window<SWEEPS, true>(work, dst, wins, item, status, done, tq, wa, trow, lane);
+}
+
+// L2 prefetch of window `item`'s rows (issued by one lane): the window the
+// warp of the CTA one wave later solves, so its staging finds it in L2.
+__device__ __forceinline__ void prefetch_window(const double* d, const BatchWin* __restrict__ wins, long long item) {
+  const long long off = __ldg(&wins[item].off);
+  const int nwin = __ldg(&wins[item].nwin);
+  const uintptr_t a = reinterpret_cast<uintptr_t>(d + off) & ~(uintptr_t)15;
+  const uintptr_t e = (reinterpret_cast<uintptr_t>(d + off + nwin) + 15) & ~(uintptr_t)15;
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)(e - a)) : "memory");
+}
+
+// The whole batch in one launch: CTAs below nft solve BW full windows (one
+// per warp), the others BW padded ones.  Each warp first prefetches into L2
+// the window of the warp pf CTAs further on (pf = the CTAs resident at once).
+template <int SWEEPS>
+__global__ void __launch_bounds__(32 * BW, 6)
+    batch_refine_kernel(double* work, double* d, const BatchWin* __restrict__ wins, int n_full, int n_pad,
+                        unsigned* status, unsigned* done, unsigned nft, unsigned pf) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int P = sys_pitch<BM>();
+  const int warp = threadIdx.x >> 5;
+  const unsigned lane = threadIdx.x & 31;
+  float4* tq = reinterpret_cast<float4*>(smem_raw) + (size_t)warp * BTAB;
+  BatchWin* wa = reinterpret_cast<BatchWin*>(reinterpret_cast<float4*>(smem_raw) + (size_t)BW * BTAB) + warp;
+  double* trow = reinterpret_cast<double*>(reinterpret_cast<BatchWin*>(reinterpret_cast<float4*>(smem_raw) +
+                                                                        (size_t)BW * BTAB) + BW) + (size_t)warp * P;
+  if (lane == 0 && pf > 0) {
+    const long long b = (long long)blockIdx.x + pf;
+    const long long it = b * BW + warp;  // windows are stored full first, then padded
+    const long long nb = (b < nft) ? it : (long long)n_full + (b - nft) * BW + warp;
+    if ((b < nft && it < n_full) || (b >= nft && nb < (long long)n_full + n_pad)) prefetch_window(d, wins, nb);
+  }
+  if (blockIdx.x < nft) {
+    const long long it = (long long)blockIdx.x * BW + warp;
+    if (it < n_full) refine_window<SWEEPS, false>(work, d, wins, it, status, done, tq, wa, trow, lane);
+  } else {
+    const long long it = (long long)(blockIdx.x - nft) * BW + warp;
+    if (it < n_pad) refine_window_padded<SWEEPS>(work, d, wins + n_full, it, status, done, tq, wa, trow, lane);
+  }
 }
 
 constexpr size_t batch_smem() {
   return (size_t)BW * BTAB * sizeof(float4) + (size_t)BW * sizeof(BatchWin) +
          (size_t)BW * sys_pitch<BM>() * sizeof(double);
-}
-
-template <int SWEEPS, bool PAD>
-int batch_launch(const double* src, double* dst, const BatchWin* wins, int nwins, unsigned* status,
-                 cudaStream_t st) {
-  if (nwins <= 0) return NTK_OK;
-  auto kern = batch_refine_kernel<SWEEPS, PAD>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_smem());
-  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(batch_refine_kernel)");
-  const unsigned blocks = (unsigned)((nwins + BW - 1) / BW);
-  kern<<<blocks, 32 * BW, batch_smem(), st>>>(src, dst, wins, nwins, status);
-  return cuda_status(cudaGetLastError(), "batch_refine_kernel");
 }
 
 }  // namespace refine_detail
@@ -243,9 +313,13 @@ struct BatchRefine {
   int n_full = 0, n_pad = 0;  // windows of 512 rows, then padded ones
   BatchWin* d_wins = nullptr;
   unsigned* d_status = nullptr;
+  unsigned* d_done = nullptr;  // per system: its windows finished in the current launch
+  unsigned nft = 0, npt = 0;   // CTAs of full and of padded windows
+  unsigned pf = 0;             // prefetch distance in CTAs (the CTAs resident at once)
   ~BatchRefine() {
     if (d_wins) cudaFree(d_wins);
     if (d_status) cudaFree(d_status);
+    if (d_done) cudaFree(d_done);
   }
 };
 
@@ -355,11 +429,14 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
         for (int k = 0; k < 3; ++k) w.td[0][k] = to_dw(tail[6 * s + 3 + k]);
         w.td[0][2] = to_dw(0.0);
       }
+      w.blo = w.out_lo;  // a whole system: no border rows
+      w.bhi = w.out_hi;
       (ns == BLW ? full : padded).push_back(w);
       continue;
     }
     const int Pm1 = (ns - BLW + H + L - 1) / L;
     const int Pw = Pm1 + 1;
+    const size_t first = full.size();
     for (int g = 0; g < Pw; ++g) {
       BatchWin w = base;
       w.nwin = BLW;
@@ -386,6 +463,18 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
       w.off = offset[s] + start;
       full.push_back(w);
     }
+    // border rows: central rows the neighbouring windows read
+    for (int g = 0; g < Pw; ++g) {
+      BatchWin& w = full[first + g];
+      w.sysi = (int)s;
+      w.wfirst = (int)first;
+      w.wcount = Pw;
+      const long long st = w.off - offset[s];
+      w.blo = w.out_lo;
+      w.bhi = w.out_hi;
+      if (g > 0) w.blo = (int)std::min<long long>(w.out_hi, full[first + g - 1].off - offset[s] + BLW - st);
+      if (g + 1 < Pw) w.bhi = (int)std::max<long long>(w.out_lo, full[first + g + 1].off - offset[s] - st);
+    }
   }
   BatchRefine* br = new (std::nothrow) BatchRefine();
   if (!br) {
@@ -406,6 +495,22 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
   }
   if (!rc) rc = cuda_status(cudaMalloc(&br->d_status, sizeof(unsigned)), "cudaMalloc(status)");
   if (!rc) rc = cuda_status(cudaMemset(br->d_status, 0, sizeof(unsigned)), "cudaMemset(status)");
+  if (!rc) rc = cuda_status(cudaMalloc(&br->d_done, sizeof(unsigned) * (size_t)nsys), "cudaMalloc(system counters)");
+  if (!rc) rc = cuda_status(cudaMemset(br->d_done, 0, sizeof(unsigned) * (size_t)nsys), "cudaMemset(system counters)");
+  if (!rc) {
+    auto kern = br->sweeps == 0 ? batch_refine_kernel<0> : batch_refine_kernel<1>;
+    rc = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_smem()),
+                     "cudaFuncSetAttribute(batch_refine_kernel)");
+    br->nft = (unsigned)((br->n_full + BW - 1) / BW);
+    br->npt = (unsigned)((br->n_pad + BW - 1) / BW);
+    int dev = 0, sms = 0, per_sm = 0;
+    if (!rc) rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if (!rc) rc = cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    if (!rc)
+      rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * BW, batch_smem()),
+                       "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    br->pf = (unsigned)(per_sm * sms);
+  }
   if (rc) {
     delete br;
     return rc;
@@ -418,20 +523,13 @@ void batch_refine_destroy(BatchRefine* br) { delete br; }
 
 long long batch_refine_windows(const BatchRefine* br) { return (long long)br->n_full + br->n_pad; }
 
-int batch_refine_solve(BatchRefine* br, double* d, double* work, long long total, cudaStream_t st) {
+int batch_refine_solve(BatchRefine* br, double* d, double* work, cudaStream_t st) {
   using namespace refine_detail;
-  // windows overlap: read from a copy, write d
-  int rc = cuda_status(cudaMemcpyAsync(work, d, sizeof(double) * (size_t)total, cudaMemcpyDeviceToDevice, st),
-                       "cudaMemcpyAsync(batch input copy)");
-  if (rc) return rc;
-  if (br->sweeps == 0) {
-    rc = batch_launch<0, false>(work, d, br->d_wins, br->n_full, br->d_status, st);
-    if (!rc) rc = batch_launch<0, true>(work, d, br->d_wins + br->n_full, br->n_pad, br->d_status, st);
-  } else {
-    rc = batch_launch<1, false>(work, d, br->d_wins, br->n_full, br->d_status, st);
-    if (!rc) rc = batch_launch<1, true>(work, d, br->d_wins + br->n_full, br->n_pad, br->d_status, st);
-  }
-  return rc;
+  if (br->n_full + br->n_pad == 0) return NTK_OK;
+  auto kern = br->sweeps == 0 ? batch_refine_kernel<0> : batch_refine_kernel<1>;
+  kern<<<br->nft + br->npt, 32 * BW, batch_smem(), st>>>(work, d, br->d_wins, br->n_full, br->n_pad, br->d_status,
+                                                         br->d_done, br->nft, br->pf);
+  return cuda_status(cudaGetLastError(), "batch_refine_kernel");
 }
 
 }  // namespace ntk

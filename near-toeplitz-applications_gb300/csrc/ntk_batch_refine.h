@@ -16,6 +16,6 @@ void batch_refine_destroy(BatchRefine* br);
 void batch_refine_status_words(const BatchRefine* br, std::vector<unsigned*>& out);
 long long batch_refine_windows(const BatchRefine* br);
 // in place on d (elements [0, total)); work: a device array of total doubles
-int batch_refine_solve(BatchRefine* br, double* d, double* work, long long total, cudaStream_t st);
+int batch_refine_solve(BatchRefine* br, double* d, double* work, cudaStream_t st);
 
 }  // namespace ntk

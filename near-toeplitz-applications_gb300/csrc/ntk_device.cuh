@@ -97,6 +97,44 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem, unsigned
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // ---------------------------------------------------------------------------
+// border rows of the batch windows (ntk_batch.cu, ntk_batch_refine.cu)
+// ---------------------------------------------------------------------------
+// Border rows of windows g = first .. first + count - 1 copied from work into
+// d by one warp (geom(g, base, lo, blo, bhi, hi): rows base + [lo, blo) and
+// base + [bhi, hi)).  Segments are short (a few dozen rows), so the warp
+// loads four windows' first 64 rows of each segment before storing any:
+// 16 loads in flight per lane instead of a chain of round trips.
+template <class GEOM>
+__device__ __forceinline__ void border_copy(const double* work, double* d, int first, int count, unsigned lane,
+                                            GEOM geom) {
+  for (int g0 = first; g0 < first + count; g0 += 4) {
+    double v[4][4];
+    long long at[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      long long base = 0;
+      int lo = 0, blo = 0, bhi = 0, hi = 0;
+      if (g0 + i < first + count) geom(g0 + i, base, lo, blo, bhi, hi);
+      const int r[4] = {lo + (int)lane, lo + 32 + (int)lane, bhi + (int)lane, bhi + 32 + (int)lane};
+      const int e[4] = {blo, blo, hi, hi};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        at[i][q] = r[q] < e[q] ? base + r[q] : -1;
+        v[i][q] = at[i][q] >= 0 ? __ldcg(work + at[i][q]) : 0.0;
+      }
+      // rows beyond 64 of a segment (long halos): plain loop
+      for (int rr = lo + 64 + (int)lane; rr < blo; rr += 32) d[base + rr] = __ldcg(work + base + rr);
+      for (int rr = bhi + 64 + (int)lane; rr < hi; rr += 32) d[base + rr] = __ldcg(work + base + rr);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (at[i][q] >= 0) d[at[i][q]] = v[i][q];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // small utilities
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }

@@ -179,3 +179,31 @@ def test_refine_rejects_slow_decay(cuda):
     hd = np.array([[[0, 1.0, 0.49], [0.49, 1.0, 0.49]]])
     with pytest.raises(Exception, match="NTK_FP64"):
         ntk.UnevenBatch([4096], inter, hd, hd, precision="fp32_refine")
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL), ("fp32_refine", 1e-12)])
+def test_repeated_solves_in_one_stream(cuda, oracle, precision, tol):
+    """Three solves of the same batch back to back: the windows' per-system
+    counters (the last window of a system copies its border rows) reset
+    themselves at the end of every launch, so each solve is complete."""
+    import ntk
+    from ntk.workloads import uneven_batch
+
+    lengths, systems = uneven_batch(256, seed=7)
+    interior, head, tail = _descriptors(lengths, systems)
+    rng = np.random.default_rng(8)
+    with ntk.UnevenBatch(lengths, interior, head, tail, precision=precision) as bt:
+        offs = bt.offsets
+        ds = [rng.normal(size=bt.elements) for _ in range(3)]
+        ts = [torch.from_numpy(d).to(cuda) for d in ds]
+        for t in ts:
+            bt.solve(t)
+        torch.cuda.synchronize()
+        assert bt.status() == 0
+    for d, t in zip(ds, ts):
+        x = t.cpu().numpy()
+        for s, n in enumerate(lengths):
+            o = int(offs[s])
+            a, b, c = _bands(int(n), interior[s], head[s], tail[s])
+            ref = oracle.thomas_ld(a, b, c, d[o:o + n])
+            assert oracle.rel_err(x[o:o + n], ref) < tol, (s, n)
