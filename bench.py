@@ -729,7 +729,7 @@ def profile_case(which):
     autotuner picks on GB300 for the benchmark: x W = 4, y W = 8, z W = 8
     with two systems per warp; FP64 defaults; y on the x field's shape), `adi` one FP32 + refine ADI step on
     2048^2 (one launch per half step; `adi_f64` the same in FP64), `batch` one FP32 + refine solve of the
-    4096-system uneven batch (two launches; `batch_f64` the FP64 windows, one
+    4096-system uneven batch (one launch; `batch_f64` the FP64 windows, one
     launch)."""
     import numpy as np
     import torch

@@ -93,14 +93,19 @@ int ntk_plan_create(ntk_plan** out, int n, long long nrhs, const double coeffs[7
  *   NTK_TUNE_REFINE_PREFETCH  the one-group strided kernel: a CTA prefetches
  *                           into L2 the tile the CTA resident p / 2 waves
  *                           later will load, p = 0 (none) .. 4; default 2
- *                           (one wave). */
+ *                           (one wave).
+ *   NTK_TUNE_REFINE_TPS     threads per system for 512 < n <= 1024: 32 (one
+ *                           warp, 32 rows per lane; 0 = default) or 64 (two
+ *                           overlapping 512-row windows, 16 rows per lane,
+ *                           where the factors decay fast enough; else 32). */
 enum ntk_tune_key {
   NTK_TUNE_F64_X_VARIANT = 1,
   NTK_TUNE_F64_THREADS = 2,
   NTK_TUNE_REFINE_W = 3,
   NTK_TUNE_REFINE_SPW = 4,
   NTK_TUNE_REFINE_KERNEL = 5,
-  NTK_TUNE_REFINE_PREFETCH = 6
+  NTK_TUNE_REFINE_PREFETCH = 6,
+  NTK_TUNE_REFINE_TPS = 7
 };
 int ntk_plan_set_tuning(ntk_plan* plan, int key, int value);
 int ntk_plan_get_tuning(const ntk_plan* plan, int key, int* value);

@@ -260,6 +260,10 @@ int ntk_plan_set_tuning(ntk_plan* plan, int key, int value) {
       if (value < 0 || value > 4) break;
       plan->tune_refine_prefetch = value;
       return NTK_OK;
+    case NTK_TUNE_REFINE_TPS:
+      if (value != 0 && value != 32 && value != 64) break;
+      plan->tune_refine_tps = value;
+      return NTK_OK;
     default:
       ntk::set_error("ntk_plan_set_tuning: unknown key %d", key);
       return NTK_ERR_INVALID;
@@ -280,6 +284,7 @@ int ntk_plan_get_tuning(const ntk_plan* plan, int key, int* value) {
     case NTK_TUNE_REFINE_SPW: *value = plan->tune_refine_spw; return NTK_OK;
     case NTK_TUNE_REFINE_KERNEL: *value = plan->tune_refine_kernel; return NTK_OK;
     case NTK_TUNE_REFINE_PREFETCH: *value = plan->tune_refine_prefetch; return NTK_OK;
+    case NTK_TUNE_REFINE_TPS: *value = plan->tune_refine_tps; return NTK_OK;
     default:
       ntk::set_error("ntk_plan_get_tuning: unknown key %d", key);
       return NTK_ERR_INVALID;

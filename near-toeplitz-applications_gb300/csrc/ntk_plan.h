@@ -72,6 +72,7 @@ struct Plan {
   RefineState* refine = nullptr;
   LongRefine* long_refine = nullptr;  // FP32 / FP32+refine windows for n > 1024
   SpikeSolver* spike = nullptr;       // n > 1024 where the windows' halos do not decay: exact partitions
+  LongRefine* long_alt = nullptr;     // 512 < n <= 1024: two-window solve (64 threads per system)
   std::mutex mu;
   // launch configuration (ntk_plan_set_tuning; chosen by the autotuner)
   int tune_f64_x_variant = 0;  // contiguous FP64 sweeps: 0 tile ring, 1 whole-system tile, 2 direct
@@ -81,6 +82,8 @@ struct Plan {
   int tune_refine_kernel = 0;  // n = 512: paired-chunk TMA kernels where they apply (0: automatic, 2: one
                                // strided group per CTA, 3: persistent strided CTAs), 1: the chunked kernel
   int tune_refine_prefetch = 2;  // one-group strided CTAs: L2 prefetch 0 .. 4 half waves ahead
+  int tune_refine_tps = 0;       // threads per system, 512 < n <= 1024: 32 (one warp, 32 rows per lane; 0 =
+                                 // automatic) or 64 (two 512-row windows, 16 rows per lane)
 
   int init(int n, long long nrhs, const double co[7], int precision, int sweeps);
   ~Plan();

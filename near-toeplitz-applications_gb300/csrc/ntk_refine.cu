@@ -69,6 +69,12 @@ int Plan::init_refine() {
   }
   st->M = M;
   st->n_pad = 32 * M;
+  if (n > 512) {
+    // the alternative for 512 < n <= 1024: two overlapping 512-row windows,
+    // 64 threads per system (NTK_TUNE_REFINE_TPS); unavailable where the
+    // factors decay too slowly for their halos
+    if (long_refine_create(&long_alt, *this, precision, sweeps) != NTK_OK) long_alt = nullptr;
+  }
   // FP32 tables in the padded chunk layout (ChunkTabs); rows >= n are
   // identity rows (l = w = 0, g = 1)
   std::vector<double> L(32 * M, 0.0), G(32 * M, 1.0), Wv(32 * M, 0.0);
@@ -186,6 +192,7 @@ void Plan::status_words(std::vector<unsigned*>& out) const {
   if (refine && refine->d_status) out.push_back(refine->d_status);
   if (long_refine) long_refine_status_words(long_refine, out);
   if (spike) spike_status_words(spike, out);
+  if (long_alt) long_refine_status_words(long_alt, out);
 }
 
 void Plan::release_refine() {
@@ -196,6 +203,10 @@ void Plan::release_refine() {
   if (spike) {
     spike_destroy(spike);
     spike = nullptr;
+  }
+  if (long_alt) {
+    long_refine_destroy(long_alt);
+    long_alt = nullptr;
   }
   if (!refine) return;
   if (refine->d_tab) cudaFree(refine->d_tab);
@@ -228,6 +239,7 @@ int Plan::run_refine(const double* in, double* out, const Batch& b, const RhsPar
     set_error("FP32/refine supports the identity and compact right-hand sides");
     return NTK_ERR_UNSUPPORTED;
   }
+  if (long_alt && tune_refine_tps == 64) return long_refine_run(long_alt, in, out, b, rp, s, tune_refine_w, stream);
   if (rp.kind == RHS_COMPACT && n < 4) {
     set_error("compact derivative needs n >= 4");
     return NTK_ERR_INVALID;

@@ -145,7 +145,9 @@ class Plan:
         self.close()
 
     def set_tuning(self, **kw):
-        """Set launch parameters: f64_x_variant, f64_threads, refine_w, refine_spw."""
+        """Set launch parameters (ntk_plan_set_tuning): f64_x_variant,
+        f64_threads, refine_w, refine_spw, refine_kernel, refine_prefetch,
+        refine_tps."""
         for k, v in kw.items():
             if k not in _lib.TUNE_KEYS:
                 raise ValueError("unknown tuning key %r" % k)

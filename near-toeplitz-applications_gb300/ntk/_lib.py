@@ -32,9 +32,11 @@ NTK_TUNE_REFINE_W = 3
 NTK_TUNE_REFINE_SPW = 4
 NTK_TUNE_REFINE_KERNEL = 5
 NTK_TUNE_REFINE_PREFETCH = 6
+NTK_TUNE_REFINE_TPS = 7
 TUNE_KEYS = {"f64_x_variant": NTK_TUNE_F64_X_VARIANT, "f64_threads": NTK_TUNE_F64_THREADS,
              "refine_w": NTK_TUNE_REFINE_W, "refine_spw": NTK_TUNE_REFINE_SPW,
-             "refine_kernel": NTK_TUNE_REFINE_KERNEL, "refine_prefetch": NTK_TUNE_REFINE_PREFETCH}
+             "refine_kernel": NTK_TUNE_REFINE_KERNEL, "refine_prefetch": NTK_TUNE_REFINE_PREFETCH,
+             "refine_tps": NTK_TUNE_REFINE_TPS}
 
 # (name, restype, argtypes) of every exported entry point, in header order
 _vp = ctypes.c_void_p

@@ -21,6 +21,10 @@ cached per (device, kernel family, n, precision, layout):
   refine_prefetch  one-group strided CTAs: L2 prefetch of the tile needed
                  p / 2 waves later (p = 1, 2, 3 searched; 0 and 4, no
                  prefetch and two waves, measured slower on every axis)
+  refine_tps     threads per system: 32 everywhere (paired-chunk kernels:
+                 16 rows per thread; chunked kernel: one warp per system);
+                 for 512 < n <= 1024 also 64 (two overlapping 512-row
+                 windows, 16 rows per lane, instead of one warp with 32)
 
 Usage:
     best = autotune.tune(plan, run, key)   # run() launches the workload once
@@ -79,9 +83,14 @@ def cache_key(plan, key):
     return "|".join([device_name(), str(plan.n), str(plan.precision), str(key)])
 
 
-def candidates(precision):
+def candidates(precision, n=None):
+    """The configurations searched for a plan of this precision and system
+    length n (threads per system: 64 only offered for 512 < n <= 1024)."""
     out = []
     for space in SPACE.get(precision, [{}]):
+        if "refine_kernel" in space:
+            tps = [32, 64] if (n is not None and 512 < n <= 1024 and space["refine_kernel"] == [1]) else [32]
+            space = dict(space, refine_tps=tps)
         configs = [{}]
         for name, values in space.items():
             configs = [dict(c, **{name: v}) for c in configs for v in values]
@@ -117,7 +126,7 @@ def tune(plan, run, key, repeats=5, timer=None, use_cache=True):
             plan.set_tuning(**hit["config"])
             return hit
     results = []
-    for cfg in candidates(plan.precision):
+    for cfg in candidates(plan.precision, getattr(plan, "n", None)):
         plan.set_tuning(**cfg)
         results.append((_time(run, repeats, timer), cfg))
     results.sort(key=lambda r: r[0])

@@ -21,11 +21,16 @@ def test_candidates_cover_the_space():
     c = autotune.candidates("fp32_refine")
     assert len(c) == 17
     for w in (4, 8, 16):
-        assert {"refine_kernel": 2, "refine_w": w, "refine_prefetch": 1} in c
-        assert {"refine_kernel": 3, "refine_w": w} in c
-    assert {"refine_kernel": 1, "refine_w": 8, "refine_spw": 2} in c
-    assert {"refine_kernel": 1, "refine_w": 16, "refine_spw": 1} in c
-    assert {"refine_kernel": 1, "refine_w": 16, "refine_spw": 2} not in c  # more than 16 systems per CTA
+        assert {"refine_kernel": 2, "refine_w": w, "refine_prefetch": 1, "refine_tps": 32} in c
+        assert {"refine_kernel": 3, "refine_w": w, "refine_tps": 32} in c
+    assert {"refine_kernel": 1, "refine_w": 8, "refine_spw": 2, "refine_tps": 32} in c
+    assert {"refine_kernel": 1, "refine_w": 16, "refine_spw": 1, "refine_tps": 32} in c
+    assert {"refine_kernel": 1, "refine_w": 16, "refine_spw": 2, "refine_tps": 32} not in c  # > 16 systems per CTA
+    # threads per system: 64 (two 512-row windows) only for 512 < n <= 1024
+    assert all(x.get("refine_tps", 32) == 32 for x in autotune.candidates("fp32_refine", 512))
+    c1024 = autotune.candidates("fp32_refine", 1024)
+    assert {"refine_kernel": 1, "refine_w": 8, "refine_spw": 1, "refine_tps": 64} in c1024
+    assert len(c1024) == 17 + 5
 
 
 def test_tune_picks_fastest_and_caches(tmp_path, monkeypatch):
@@ -36,7 +41,7 @@ def test_tune_picks_fastest_and_caches(tmp_path, monkeypatch):
     plan = FakePlan("fp32_refine")
     fake_ms = {(1, 4, 1): 2.0, (1, 8, 1): 1.0, (1, 16, 1): 0.75, (1, 4, 2): 1.5, (1, 8, 2): 0.5,
                (3, 4, 1): 0.9, (3, 8, 1): 0.6, (3, 16, 1): 0.7, (2, 4, 1): 0.95, (2, 8, 1): 0.65, (2, 16, 1): 0.8}
-    best = {"refine_kernel": 1, "refine_w": 8, "refine_spw": 2}
+    best = {"refine_kernel": 1, "refine_w": 8, "refine_spw": 2, "refine_tps": 32}
 
     def timer(run, repeats):
         c = plan.cfg

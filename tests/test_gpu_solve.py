@@ -232,3 +232,29 @@ def test_refine_long_systems(cuda, oracle, cname, n):
     assert oracle.rel_err(x, _banded(oracle, n, co, d)) < REFINE_TOL
     x32 = _solve(cuda, n, 9, co, d, precision="fp32")
     assert oracle.rel_err(x32, _banded(oracle, n, co, d)) < 2e-5
+
+
+@pytest.mark.parametrize("n", [600, 700, 1024])
+@pytest.mark.parametrize("tps", [32, 64])
+def test_refine_threads_per_system(cuda, oracle, n, tps):
+    """512 < n <= 1024: one warp per system (32 threads, 32 rows per lane) or
+    two overlapping 512-row windows (64 threads, 16 rows per lane), for the
+    plain solve and the compact derivative: both within 1e-12."""
+    import ntk
+
+    co = COEFF_SETS["compact"]
+    nrhs = 48
+    rng = np.random.default_rng(n + tps)
+    d = rng.standard_normal((nrhs, n))
+    t = torch.from_numpy(d.copy()).to(cuda)
+    with ntk.Plan(n, nrhs, co, precision="fp32_refine") as p:
+        p.set_tuning(refine_tps=tps)
+        p.solve(t)
+        f = torch.from_numpy(rng.standard_normal((1, nrhs, n))).to(cuda)
+        out = torch.empty_like(f)
+        p.compact_deriv(f, out, axis=2, h=1.0 / (n - 1))
+        torch.cuda.synchronize()
+    ref = _banded(oracle, n, co, d)
+    assert oracle.rel_err(t.cpu().numpy(), ref) < REFINE_TOL
+    dref = oracle.banded_compact_deriv(f.cpu().numpy(), 1.0 / (n - 1), axis=2)
+    assert oracle.rel_err(out.cpu().numpy(), dref) < REFINE_TOL
