@@ -730,7 +730,8 @@ def profile_case(which):
     with two systems per warp; FP64 defaults; y on the x field's shape), `adi` one FP32 + refine ADI step on
     2048^2 (one launch per half step; `adi_f64` the same in FP64), `batch` one FP32 + refine solve of the
     4096-system uneven batch (one launch; `batch_f64` the FP64 windows, one
-    launch)."""
+    launch), `grad` one ntk_compact_grad call (one launch) on the 512^3 field
+    (4 GiB on the device: for one-pass metrics only)."""
     import numpy as np
     import torch
 
@@ -745,6 +746,15 @@ def profile_case(which):
               "chunked_z": {"refine_kernel": 1, "refine_w": 8, "refine_spw": 2}}
     fields = {}
     for w in which:
+        if w == "grad":
+            f = fourier_field((512, 512, 512), seed=0, device=dev)
+            outs = [torch.empty_like(f) for _ in range(3)]
+            with ntk.Plan(512, 0, COMPACT_COEFFS, precision="fp32_refine") as p:
+                for _ in range(2):
+                    p.compact_grad(f, outs[0], outs[1], outs[2], h=1.0 / 511)
+            torch.cuda.synchronize()
+            del f, outs
+            continue
         if w in ("adi", "adi_f64"):
             NA = 2048
             dx = 1.0 / (NA - 1)
@@ -799,7 +809,8 @@ def main():
     ap.add_argument("--profile-case", default=None,
                     help="comma list of refine_x,refine_y,refine_z (paired-chunk kernels), chunked_x,chunked_y,chunked_z, "
                          "fp64_x,fp64_z,adi,adi_f64,batch,batch_f64: two launches each on ~256 MiB fields "
-                         "(n = 512 along the solved axis), for ncu captures; prints nothing to time")
+                         "(n = 512 along the solved axis), grad: two one-launch gradients of the 512^3 field; "
+                         "for ncu captures; prints nothing to time")
     args = ap.parse_args()
     if args.profile_case:
         return profile_case(args.profile_case.split(","))
