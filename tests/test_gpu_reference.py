@@ -98,3 +98,49 @@ def test_compact_derivative_vs_reference_kernels(ref_gpu, oracle, cuda, axis):
             p.compact_deriv(ft, out, axis=axis, h=h)
         torch.cuda.synchronize()
         assert oracle.rel_err(out.cpu().numpy(), ref.cpu().numpy()) < tol, prec
+
+
+@pytest.fixture(scope="module")
+def field_512(cuda):
+    import ntk  # noqa: F401  (loads the library before the first launch)
+    from ntk.workloads import fourier_field
+
+    return fourier_field((512, 512, 512), seed=0, device=cuda)
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_compact_derivative_vs_reference_kernels_512cube(ref_gpu, oracle, cuda, field_512, axis):
+    """The benchmark's workload at full size (run-compact.py:47-90 on a 512^3
+    field, 262144 systems of n = 512 per axis) on the reference's kernels,
+    every row compared with the ntk derivative in both precisions."""
+    import ntk
+
+    n = 512
+    h = 1.0 / (n - 1)
+    ft = field_512
+    s = torch.cuda.current_stream().cuda_stream
+    st = [n * n, n, 1]
+    ref = torch.empty_like(ft)
+    tmp = torch.empty_like(ft)
+    solver = RefSolver(ref_gpu, oracle, n, n * n, COMPACT, cuda)
+    if axis == 2:
+        assert ref_gpu.ntkref_gpu_compact_rhs(ft.data_ptr(), ref.data_ptr(), n, n, n, h, s) == 0
+        solver.solve(ref)
+    else:
+        p_in, p_out = ((0, 2, 1), (0, 2, 1)) if axis == 1 else ((1, 2, 0), (2, 0, 1))
+        ss = [st[i] for i in p_in]
+        assert ref_gpu.ntkref_gpu_permute(ft.data_ptr(), ref.data_ptr(), n, n, n, ss[0], ss[1], ss[2], s) == 0
+        assert ref_gpu.ntkref_gpu_compact_rhs(ref.data_ptr(), tmp.data_ptr(), n, n, n, h, s) == 0
+        solver.solve(tmp)
+        ss = [st[i] for i in p_out]
+        assert ref_gpu.ntkref_gpu_permute(tmp.data_ptr(), ref.data_ptr(), n, n, n, ss[0], ss[1], ss[2], s) == 0
+    del tmp
+    scale = ref.abs().max()
+    for prec, tol in (("fp64", 1e-13), ("fp32_refine", 1e-12)):
+        out = torch.empty_like(ft)
+        with ntk.Plan(n, 0, COMPACT, precision=prec) as p:
+            p.compact_deriv(ft, out, axis=axis, h=h)
+        torch.cuda.synchronize()
+        err = ((out - ref).abs().max() / scale).item()
+        assert err < tol, (prec, err)
+        del out
