@@ -305,11 +305,20 @@ int ntk_batch_status(ntk_batch* batch, int* flags, void* stream);
  * elements the data buffer must span. */
 int ntk_batch_info(const ntk_batch* batch, long long* max_n, long long* segmented, long long* elements);
 
+/* Windows the batch solves (512 rows each, one warp per window; 0 on the
+ * one-warp-per-system FP64 path) and, for NTK_FP32_REFINE / NTK_FP32, how
+ * many of them take the paired-chunk FP32 solve (constant Toeplitz factors
+ * with end corrections; the others, and systems shorter than 512 rows, take
+ * the chunked solve with per-window factor tables). */
+int ntk_batch_windows(const ntk_batch* batch, long long* windows, long long* paired);
+
 /* Solves every system in place in d (device), asynchronously on `stream`:
- * windows (FP64 windows, NTK_FP32_REFINE, NTK_FP32) are one device-to-device
- * copy of d into the work array and one launch per window class; the
- * one-warp-per-system FP64 kernel is one launch preceded by a 4-byte memset
- * of its work counter.  Graph-capturable. */
+ * windows (FP64 windows, NTK_FP32_REFINE, NTK_FP32) are one kernel launch
+ * (each window reads its rows from d and writes its central rows back; the
+ * rows a neighbouring window reads go through the work array until the
+ * system's last window copies them in); the one-warp-per-system FP64 kernel
+ * is one launch preceded by a 4-byte memset of its work counter.
+ * Graph-capturable. */
 int ntk_batch_solve(ntk_batch* batch, double* d, void* stream);
 
 #ifdef __cplusplus

@@ -733,6 +733,23 @@ int ntk_batch_info(const ntk_batch* b, long long* max_n, long long* segmented, l
   return NTK_OK;
 }
 
+int ntk_batch_windows(const ntk_batch* b, long long* windows, long long* paired) {
+  if (!b) {
+    ntk::set_error("ntk_batch_windows: null batch");
+    return NTK_ERR_INVALID;
+  }
+  long long w = 0, p = 0;
+  if (b->refine) {
+    w = ntk::batch_refine_windows(b->refine);
+    p = ntk::batch_refine_paired_windows(b->refine);
+  } else if (b->d_wins) {
+    w = b->nwin;
+  }
+  if (windows) *windows = w;
+  if (paired) *paired = p;
+  return NTK_OK;
+}
+
 int ntk_batch_solve(ntk_batch* b, double* d, void* stream) {
   if (!b || !d || (reinterpret_cast<uintptr_t>(d) & 7)) {
     ntk::set_error("ntk_batch_solve: null batch or null/misaligned d");

@@ -28,6 +28,8 @@
 #include <vector>
 
 #include "ntk_batch_refine.h"
+#include "ntk_r2_group.cuh"
+#include "ntk_r2_host.h"
 #include "ntk_refine.cuh"
 
 namespace ntk {
@@ -50,6 +52,7 @@ struct BatchWin {
   int blo = 0, bhi = 0;
   int sysi = 0;                // the system's counter
   int wfirst = 0, wcount = 1;  // the system's windows
+  int args = -1;               // paired-chunk windows: index of the kind's constants
 };
 
 namespace refine_detail {
@@ -62,6 +65,7 @@ constexpr int BW = 4;                   // warps (windows) per CTA
 // slot: 0 lane 0 (the window's head), 1 interior lanes, 2..4 the lanes
 // around the system's tail rows, 5 lanes wholly in the padding.
 constexpr int BSLOTS = 6;
+constexpr int NROWS_R2 = 512;           // rows of a paired-chunk window
 constexpr int BTAB = BSLOTS * class_pitch4<BM>();  // float4s of one warp's tables
 
 __device__ __forceinline__ void row_coeffs(const BatchWin& w, int r, float& a, float& b, float& c) {
@@ -251,14 +255,87 @@ __device__ __forceinline__ void refine_window(double* work, double* dst, const B
   if (w.wcount > 1) finish_system(work, dst, wins, w, done, lane);
 }
 
-// The padded windows' solve as a separate (not inlined) function: one
-// kernel holding both window kinds inline spills heavily; the full windows,
-// most of the rows, stay inline.
+// The chunked path's windows as separate (not inlined) functions: one kernel
+// holding them inline beside the paired-chunk windows spills heavily.
+template <int SWEEPS, bool PAD>
+__device__ __noinline__ void refine_window_call(double* work, double* dst, const BatchWin* __restrict__ wins,
+                                                long long item, unsigned* status, unsigned* done, float4* tq,
+                                                BatchWin* wa, double* trow, unsigned lane) {
+  refine_window<SWEEPS, PAD>(work, dst, wins, item, status, done, tq, wa, trow, lane);
+}
+
+// A full window whose system qualifies for the paired-chunk solve
+// (ntk_r2_group.cuh): the FP32 solve of the pure Toeplitz matrix with the
+// window kind's Woodbury end corrections (Args, computed on the host once per
+// batch and copied into shared memory), interior coefficients of any value
+// in the residual.  The warp stages its 512 rows with 8-byte copies into a
+// 4 KB tile in the 128-byte-swizzled layout the solve reads (rows 2i, 2i + 1
+// of chunk j at xpair(j, i)), rewrites them as (hi, lo) pairs, solves, puts
+// the results back into the tile and stores the window's central rows with
+// coalesced stores (border rows to work, as in refine_window).
 template <int SWEEPS>
-__device__ __noinline__ void refine_window_padded(double* work, double* dst, const BatchWin* __restrict__ wins,
-                                                  long long item, unsigned* status, unsigned* done, float4* tq,
-                                                  BatchWin* wa, double* trow, unsigned lane) {
-  refine_window<SWEEPS, true>(work, dst, wins, item, status, done, tq, wa, trow, lane);
+__device__ __forceinline__ void r2_window(double* work, double* dst, const BatchWin* __restrict__ wins,
+                                          const r2::Args* __restrict__ args, long long item, unsigned* status,
+                                          unsigned* done, r2::Args* sa, double* tile, unsigned lane) {
+  const BatchWin* wp = wins + item;
+  const long long off = __ldg(&wp->off);
+  {
+    const unsigned long long* g = reinterpret_cast<const unsigned long long*>(args + __ldg(&wp->args));
+    unsigned long long* sd = reinterpret_cast<unsigned long long*>(sa);
+    constexpr int NA = (int)(sizeof(r2::Args) / sizeof(unsigned long long));
+    for (int i = (int)lane; i < NA; i += 32) sd[i] = __ldg(g + i);
+  }
+  {
+    const double* src = dst + off;
+#pragma unroll
+    for (int q = 0; q < BM; ++q) {
+      const int r = (int)lane + 32 * q;
+      cp_async8(tile + r2::xpair(r >> 4, (r & 15) >> 1) + (r & 1), src + r, 8u);
+    }
+  }
+  cp_async_wait_all();
+  __syncwarp();
+  const int j = (int)lane;
+  unsigned rmax = 0;
+  float2 v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const double2 q = *reinterpret_cast<const double2*>(tile + r2::xpair(j, i));
+    float h0, l0, h1, l1;
+    r2::split_f64(q.x, h0, l0, rmax);
+    r2::split_f64(q.y, h1, l1, rmax);
+    if (SWEEPS > 0) *reinterpret_cast<float4*>(tile + r2::xpair(j, i)) = make_float4(h0, l0, h1, l1);
+    if (i < 4) {
+      v[2 * i].x = h0;
+      v[2 * i + 1].x = h1;
+    } else {
+      v[2 * i - 8].y = h0;
+      v[2 * i - 7].y = h1;
+    }
+  }
+  r2::contiguous_solve<SWEEPS, true>(v, tile, j, *sa, [&](int i, double oa0, double oa1, double ob0, double ob1) {
+    *reinterpret_cast<double2*>(tile + r2::xpair(j, i)) = make_double2(oa0, oa1);
+    *reinterpret_cast<double2*>(tile + r2::xpair(j, i + 4)) = make_double2(ob0, ob1);
+  });
+  __syncwarp();
+  {
+    const int lo = __ldg(&wp->out_lo), hi = __ldg(&wp->out_hi);
+    const int blo = __ldg(&wp->blo), bhi = __ldg(&wp->bhi);
+#pragma unroll 4
+    for (int q = 0; q < BM; ++q) {
+      const int r = (int)lane + 32 * q;
+      if (r >= lo && r < hi)
+        ((r < blo || r >= bhi) ? work : dst)[off + r] = tile[r2::xpair(r >> 4, (r & 15) >> 1) + (r & 1)];
+    }
+  }
+  if (__any_sync(0xffffffffu, rmax >= r2::RANGE_MAG) && lane == 0 && status) atomicOr(status, 1u);
+  if (__ldg(&wp->wcount) > 1) {
+    BatchWin w;
+    w.sysi = __ldg(&wp->sysi);
+    w.wfirst = __ldg(&wp->wfirst);
+    w.wcount = __ldg(&wp->wcount);
+    finish_system(work, dst, wins, w, done, lane);
+  }
 }
 
 // L2 prefetch of window `item`'s rows (issued by one lane): the window the
@@ -271,53 +348,104 @@ __device__ __forceinline__ void prefetch_window(const double* d, const BatchWin*
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)(e - a)) : "memory");
 }
 
-// The whole batch in one launch: CTAs below nft solve BW full windows (one
-// per warp), the others BW padded ones.  Each warp first prefetches into L2
-// the window of the warp pf CTAs further on (pf = the CTAs resident at once).
+// The launch's windows: n_r2 paired-chunk windows, then n_old full windows
+// of the chunked path (together the full array, one system's windows next
+// to each other), then n_pad padded windows; BW per CTA, CTAs [0, c_r2) on
+// the first kind, [c_r2, c_r2 + c_old) on the second, the rest on the third.
+// (Running the slower chunked windows first measured slower: 0.081 against
+// 0.075 ms for the 4096-system batch; at the end they run with fewer warps
+// beside them.)
+struct BatchGeo {
+  int n_r2 = 0, n_old = 0, n_pad = 0;
+  unsigned c_r2 = 0, c_old = 0;
+  unsigned pf = 0;  // prefetch distance in CTAs (the CTAs resident at once)
+};
+
+// Index in wins of warp `warp`'s window in CTA b, kind 0 / 1 / 2 (paired
+// chunk / chunked full / padded); -1: none.
+__device__ __forceinline__ long long window_of(long long b, int warp, const BatchGeo& g, int& kind) {
+  if (b < g.c_r2) {
+    kind = 0;
+    const long long it = b * BW + warp;
+    return it < g.n_r2 ? it : -1;
+  }
+  b -= g.c_r2;
+  if (b < g.c_old) {
+    kind = 1;
+    const long long it = b * BW + warp;
+    return it < g.n_old ? g.n_r2 + it : -1;
+  }
+  b -= g.c_old;
+  kind = 2;
+  const long long it = b * BW + warp;
+  return it < g.n_pad ? (long long)g.n_r2 + g.n_old + it : -1;
+}
+
+// shared memory of a paired-chunk CTA: BW tiles of 512 rows, then BW Args
+constexpr size_t R2_ARGS_BYTES = (sizeof(r2::Args) + 15) / 16 * 16;
+constexpr size_t r2_smem() { return (size_t)BW * NROWS_R2 * sizeof(double) + (size_t)BW * R2_ARGS_BYTES; }
+
+// CTAs per SM the kernel is compiled for (registers per thread: 65536 /
+// (32 BW x this)); a build flag, for tuning experiments.
+#ifndef NTK_BATCH_MINB
+#define NTK_BATCH_MINB 6
+#endif
+
+// The whole batch in one launch.  Each warp first prefetches into L2 the
+// window of the warp pf CTAs further on (pf = the CTAs resident at once).
 template <int SWEEPS>
-__global__ void __launch_bounds__(32 * BW, 6)
-    batch_refine_kernel(double* work, double* d, const BatchWin* __restrict__ wins, int n_full, int n_pad,
-                        unsigned* status, unsigned* done, unsigned nft, unsigned pf) {
+__global__ void __launch_bounds__(32 * BW, NTK_BATCH_MINB)
+    batch_refine_kernel(double* work, double* d, const BatchWin* __restrict__ wins,
+                        const r2::Args* __restrict__ args, unsigned* status, unsigned* done,
+                        const __grid_constant__ BatchGeo g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int P = sys_pitch<BM>();
   const int warp = threadIdx.x >> 5;
   const unsigned lane = threadIdx.x & 31;
+  if (lane == 0 && g.pf > 0) {
+    int k;
+    const long long nb = window_of((long long)blockIdx.x + g.pf, warp, g, k);
+    if (nb >= 0) prefetch_window(d, wins, nb);
+  }
+  int kind;
+  const long long it = window_of(blockIdx.x, warp, g, kind);
+  if (it < 0) return;
+  if (kind == 0) {
+    double* tile = reinterpret_cast<double*>(smem_raw) + (size_t)warp * NROWS_R2;
+    r2::Args* sa = reinterpret_cast<r2::Args*>(smem_raw + (size_t)BW * NROWS_R2 * sizeof(double) +
+                                               (size_t)warp * R2_ARGS_BYTES);
+    r2_window<SWEEPS>(work, d, wins, args, it, status, done, sa, tile, lane);
+    return;
+  }
   float4* tq = reinterpret_cast<float4*>(smem_raw) + (size_t)warp * BTAB;
   BatchWin* wa = reinterpret_cast<BatchWin*>(reinterpret_cast<float4*>(smem_raw) + (size_t)BW * BTAB) + warp;
   double* trow = reinterpret_cast<double*>(reinterpret_cast<BatchWin*>(reinterpret_cast<float4*>(smem_raw) +
                                                                         (size_t)BW * BTAB) + BW) + (size_t)warp * P;
-  if (lane == 0 && pf > 0) {
-    const long long b = (long long)blockIdx.x + pf;
-    const long long it = b * BW + warp;  // windows are stored full first, then padded
-    const long long nb = (b < nft) ? it : (long long)n_full + (b - nft) * BW + warp;
-    if ((b < nft && it < n_full) || (b >= nft && nb < (long long)n_full + n_pad)) prefetch_window(d, wins, nb);
-  }
-  if (blockIdx.x < nft) {
-    const long long it = (long long)blockIdx.x * BW + warp;
-    if (it < n_full) refine_window<SWEEPS, false>(work, d, wins, it, status, done, tq, wa, trow, lane);
-  } else {
-    const long long it = (long long)(blockIdx.x - nft) * BW + warp;
-    if (it < n_pad) refine_window_padded<SWEEPS>(work, d, wins + n_full, it, status, done, tq, wa, trow, lane);
-  }
+  if (kind == 1)
+    refine_window_call<SWEEPS, false>(work, d, wins, it, status, done, tq, wa, trow, lane);
+  else
+    refine_window_call<SWEEPS, true>(work, d, wins, it, status, done, tq, wa, trow, lane);
 }
 
 constexpr size_t batch_smem() {
-  return (size_t)BW * BTAB * sizeof(float4) + (size_t)BW * sizeof(BatchWin) +
-         (size_t)BW * sys_pitch<BM>() * sizeof(double);
+  return std::max((size_t)BW * BTAB * sizeof(float4) + (size_t)BW * sizeof(BatchWin) +
+                      (size_t)BW * sys_pitch<BM>() * sizeof(double),
+                  r2_smem());
 }
 
 }  // namespace refine_detail
 
 struct BatchRefine {
   int sweeps = 1;
-  int n_full = 0, n_pad = 0;  // windows of 512 rows, then padded ones
+  refine_detail::BatchGeo geo;
+  unsigned ctas = 0;
   BatchWin* d_wins = nullptr;
+  r2::Args* d_args = nullptr;  // the paired-chunk window kinds' constants
   unsigned* d_status = nullptr;
   unsigned* d_done = nullptr;  // per system: its windows finished in the current launch
-  unsigned nft = 0, npt = 0;   // CTAs of full and of padded windows
-  unsigned pf = 0;             // prefetch distance in CTAs (the CTAs resident at once)
   ~BatchRefine() {
     if (d_wins) cudaFree(d_wins);
+    if (d_args) cudaFree(d_args);
     if (d_status) cudaFree(d_status);
     if (d_done) cudaFree(d_done);
   }
@@ -377,7 +505,19 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
     H = (H + 3) & ~1;
   }
   const int L = BLW - 2 * H;
-  std::vector<BatchWin> full, padded;
+  // Full windows of systems whose window kinds all qualify for the
+  // paired-chunk solve go to r2w (their kinds' constants in r2args), the
+  // other full windows to full, short systems to padded.  Limits: with
+  // refinement the FP32 solve's truncations may reach 2^-22 (one sweep then
+  // leaves ~2^-44); the FP32-only precision keeps the compact plans' limits.
+  r2::PrepareLimits lim;
+  lim.general = true;
+  if (precision != NTK_FP32) {
+    lim.carry = std::ldexp(1.0, -22);
+    lim.trunc = std::ldexp(1.0, -22);
+  }
+  std::vector<BatchWin> r2w, full, padded;
+  std::vector<r2::Args> r2args;
   for (long long s = 0; s < nsys; ++s) {
     const int ns = n[s];
     BatchWin base;
@@ -387,6 +527,7 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
     base.ci = to_dw(interior[3 * s + 2]);
     base.s = to_dw(1.0);
     base.unit_scale = 1;
+    base.sysi = (int)s;
     // the system's own head rows (0, 1) and tail rows (n-2, n-1); for n = 3
     // the middle row is head's second row (ntk_batch_create's rule)
     auto set_head = [&](BatchWin& w) {
@@ -415,7 +556,7 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
       w.td[0][1] = base.bi;
       w.td[0][2] = to_dw(0.0);
     };
-    if (ns <= BLW) {
+    if (ns < BLW) {
       BatchWin w = base;
       w.off = offset[s];
       w.nwin = ns;
@@ -431,60 +572,134 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
       }
       w.blo = w.out_lo;  // a whole system: no border rows
       w.bhi = w.out_hi;
-      (ns == BLW ? full : padded).push_back(w);
+      padded.push_back(w);
       continue;
     }
-    const int Pm1 = (ns - BLW + H + L - 1) / L;
-    const int Pw = Pm1 + 1;
-    const size_t first = full.size();
-    for (int g = 0; g < Pw; ++g) {
+    // windows of 512 rows: one whole window, or first, middle..., last
+    // overlapping by the halos
+    std::vector<BatchWin> sw;
+    if (ns == BLW) {
       BatchWin w = base;
+      w.off = offset[s];
       w.nwin = BLW;
-      int start;
-      if (g == 0) {
-        start = 0;
-        w.out_lo = 0;
-        w.out_hi = L;
-        set_head(w);
-        cut_tail(w);
-      } else if (g < Pw - 1) {
-        start = g * L - H;
-        w.out_lo = H;
-        w.out_hi = H + L;
-        cut_head(w);
-        cut_tail(w);
-      } else {
-        start = ns - BLW;
-        w.out_lo = (Pw - 1) * L - start;
-        w.out_hi = BLW;
-        cut_head(w);
-        set_tail(w, BLW);
+      w.out_lo = 0;
+      w.out_hi = BLW;
+      set_head(w);
+      set_tail(w, BLW);
+      sw.push_back(w);
+    } else {
+      const int Pw = (ns - BLW + H + L - 1) / L + 1;
+      for (int g = 0; g < Pw; ++g) {
+        BatchWin w = base;
+        w.nwin = BLW;
+        int start;
+        if (g == 0) {
+          start = 0;
+          w.out_lo = 0;
+          w.out_hi = L;
+          set_head(w);
+          cut_tail(w);
+        } else if (g < Pw - 1) {
+          start = g * L - H;
+          w.out_lo = H;
+          w.out_hi = H + L;
+          cut_head(w);
+          cut_tail(w);
+        } else {
+          start = ns - BLW;
+          w.out_lo = (Pw - 1) * L - start;
+          w.out_hi = BLW;
+          cut_head(w);
+          set_tail(w, BLW);
+        }
+        w.off = offset[s] + start;
+        sw.push_back(w);
       }
-      w.off = offset[s] + start;
-      full.push_back(w);
     }
     // border rows: central rows the neighbouring windows read
+    const int Pw = (int)sw.size();
     for (int g = 0; g < Pw; ++g) {
-      BatchWin& w = full[first + g];
-      w.sysi = (int)s;
-      w.wfirst = (int)first;
+      BatchWin& w = sw[g];
       w.wcount = Pw;
       const long long st = w.off - offset[s];
       w.blo = w.out_lo;
       w.bhi = w.out_hi;
-      if (g > 0) w.blo = (int)std::min<long long>(w.out_hi, full[first + g - 1].off - offset[s] + BLW - st);
-      if (g + 1 < Pw) w.bhi = (int)std::max<long long>(w.out_lo, full[first + g + 1].off - offset[s] - st);
+      if (g > 0) w.blo = (int)std::min<long long>(w.out_hi, sw[g - 1].off - offset[s] + BLW - st);
+      if (g + 1 < Pw) w.bhi = (int)std::max<long long>(w.out_lo, sw[g + 1].off - offset[s] - st);
+    }
+    // the paired-chunk constants of the system's window kinds (first,
+    // middle, last, or whole): head rows cut (row 0 = (0, b, c)) or the
+    // system's own, tail rows the system's own or none (the interior row
+    // with c dropped, as the Toeplitz matrix has it)
+    int kinds[3] = {-1, -1, -1};  // index in r2args of: the first (or whole), a middle, the last window
+    bool ok = true;
+    for (int g = 0; g < Pw && ok; ++g) {
+      const int kind = (g == 0) ? 0 : (g == Pw - 1 ? 2 : 1);
+      if (kinds[kind] >= 0) {
+        sw[g].args = kinds[kind];
+        continue;
+      }
+      r2::MatrixRows m;
+      m.n = BLW;
+      m.ai = interior[3 * s];
+      m.bi = interior[3 * s + 1];
+      m.ci = interior[3 * s + 2];
+      if (g == 0) {
+        m.nh = 2;
+        for (int r = 0; r < 2; ++r)
+          for (int k = 0; k < 3; ++k) m.head[r][k] = head[6 * s + 3 * r + k];
+        m.head[0][0] = 0.0;
+      } else {
+        m.nh = 1;
+        m.head[0][0] = 0.0;
+        m.head[0][1] = m.bi;
+        m.head[0][2] = m.ci;
+      }
+      if (g == Pw - 1) {
+        m.nt = 2;
+        for (int r = 0; r < 2; ++r)
+          for (int k = 0; k < 3; ++k) m.tail[r][k] = tail[6 * s + 3 * r + k];
+        m.tail[1][2] = 0.0;
+      } else {
+        m.nt = 0;
+      }
+      r2::Args a;
+      if (!r2::prepare(m, &a, nullptr, lim)) {
+        ok = false;
+        break;
+      }
+      a.status = nullptr;
+      kinds[kind] = (int)r2args.size();
+      sw[g].args = kinds[kind];
+      r2args.push_back(a);
+    }
+    if (!ok) {
+      // unused constants of this system stay in r2args (harmless)
+      for (BatchWin& w : sw) w.args = -1;
+    }
+    std::vector<BatchWin>& dst = ok ? r2w : full;
+    const int first = (int)dst.size();
+    for (BatchWin& w : sw) {
+      w.wfirst = first;  // the chunked path's indices move past r2w below
+      dst.push_back(w);
     }
   }
+  for (BatchWin& w : full) w.wfirst += (int)r2w.size();
   BatchRefine* br = new (std::nothrow) BatchRefine();
   if (!br) {
     set_error("out of host memory");
     return NTK_ERR_ALLOC;
   }
   br->sweeps = (precision == NTK_FP32) ? 0 : 1;
-  br->n_full = (int)full.size();
-  br->n_pad = (int)padded.size();
-  std::vector<BatchWin> all(full);
+  BatchGeo& geo = br->geo;
+  geo.n_r2 = (int)r2w.size();
+  geo.n_old = (int)full.size();
+  geo.n_pad = (int)padded.size();
+  geo.c_r2 = (unsigned)((geo.n_r2 + BW - 1) / BW);
+  geo.c_old = (unsigned)((geo.n_old + BW - 1) / BW);
+  br->ctas = geo.c_r2 + geo.c_old + (unsigned)((geo.n_pad + BW - 1) / BW);
+  std::vector<BatchWin> all(r2w);
+  all.insert(all.end(), full.begin(), full.end());
   all.insert(all.end(), padded.begin(), padded.end());
   int rc = NTK_OK;
   if (!all.empty()) {
@@ -492,6 +707,13 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
     if (!rc)
       rc = cuda_status(cudaMemcpy(br->d_wins, all.data(), sizeof(BatchWin) * all.size(), cudaMemcpyHostToDevice),
                        "cudaMemcpy(batch windows)");
+  }
+  if (!rc && !r2args.empty()) {
+    rc = cuda_status(cudaMalloc(&br->d_args, sizeof(r2::Args) * r2args.size()), "cudaMalloc(window constants)");
+    if (!rc)
+      rc = cuda_status(
+          cudaMemcpy(br->d_args, r2args.data(), sizeof(r2::Args) * r2args.size(), cudaMemcpyHostToDevice),
+          "cudaMemcpy(window constants)");
   }
   if (!rc) rc = cuda_status(cudaMalloc(&br->d_status, sizeof(unsigned)), "cudaMalloc(status)");
   if (!rc) rc = cuda_status(cudaMemset(br->d_status, 0, sizeof(unsigned)), "cudaMemset(status)");
@@ -501,15 +723,13 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
     auto kern = br->sweeps == 0 ? batch_refine_kernel<0> : batch_refine_kernel<1>;
     rc = cuda_status(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)batch_smem()),
                      "cudaFuncSetAttribute(batch_refine_kernel)");
-    br->nft = (unsigned)((br->n_full + BW - 1) / BW);
-    br->npt = (unsigned)((br->n_pad + BW - 1) / BW);
     int dev = 0, sms = 0, per_sm = 0;
     if (!rc) rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
     if (!rc) rc = cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
     if (!rc)
       rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * BW, batch_smem()),
                        "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    br->pf = (unsigned)(per_sm * sms);
+    geo.pf = (unsigned)(per_sm * sms);
   }
   if (rc) {
     delete br;
@@ -521,14 +741,17 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
 
 void batch_refine_destroy(BatchRefine* br) { delete br; }
 
-long long batch_refine_windows(const BatchRefine* br) { return (long long)br->n_full + br->n_pad; }
+long long batch_refine_windows(const BatchRefine* br) {
+  return (long long)br->geo.n_r2 + br->geo.n_old + br->geo.n_pad;
+}
+
+long long batch_refine_paired_windows(const BatchRefine* br) { return br->geo.n_r2; }
 
 int batch_refine_solve(BatchRefine* br, double* d, double* work, cudaStream_t st) {
   using namespace refine_detail;
-  if (br->n_full + br->n_pad == 0) return NTK_OK;
+  if (br->ctas == 0) return NTK_OK;
   auto kern = br->sweeps == 0 ? batch_refine_kernel<0> : batch_refine_kernel<1>;
-  kern<<<br->nft + br->npt, 32 * BW, batch_smem(), st>>>(work, d, br->d_wins, br->n_full, br->n_pad, br->d_status,
-                                                         br->d_done, br->nft, br->pf);
+  kern<<<br->ctas, 32 * BW, batch_smem(), st>>>(work, d, br->d_wins, br->d_args, br->d_status, br->d_done, br->geo);
   return cuda_status(cudaGetLastError(), "batch_refine_kernel");
 }
 

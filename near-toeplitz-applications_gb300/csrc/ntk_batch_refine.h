@@ -15,6 +15,8 @@ void batch_refine_destroy(BatchRefine* br);
 // the status word of the window kernels
 void batch_refine_status_words(const BatchRefine* br, std::vector<unsigned*>& out);
 long long batch_refine_windows(const BatchRefine* br);
+// of those, the windows on the paired-chunk solve
+long long batch_refine_paired_windows(const BatchRefine* br);
 // in place on d (elements [0, total)); work: a device array of total doubles
 int batch_refine_solve(BatchRefine* br, double* d, double* work, cudaStream_t st);
 

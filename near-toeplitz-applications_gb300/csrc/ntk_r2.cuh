@@ -278,6 +278,9 @@ struct DWc {
 struct Args {
   Consts k;
   float2 ca, cb, cc;  // interior coefficients of A (powers of two or zero), as pairs
+  // interior coefficients of any value (res_pair_gen): their low parts and
+  // negated high parts; the low parts are zero for powers of two
+  float2 cal, cbl, ccl, nca, ncb, ncc;
   int nh, nt;         // special rows of A: head 0..nh-1, tail n-nt..n-1
   DWc hd[2][3];       // head rows (a, b, c), double-word
   DWc td[2][3];       // tail rows (a, b, c), td[nt-1] is row n-1
@@ -378,6 +381,25 @@ R2_HD float2 res_pair(float2 dh, float2 dl, float2 xm, float2 x0, float2 xp, con
   two_sum2(pb, s, p, ep);
   const float2 tail = fsub2(dl, fadd2(ep, es));
   return fadd2(fsub2(dh, p), tail);
+}
+// The same for interior coefficients of any value, each a double-word
+// (hi + lo): the high parts' product errors from FMAs (exact), the low
+// parts' products added into the tail.
+R2_HD float2 res_pair_gen(float2 dh, float2 dl, float2 xm, float2 x0, float2 xp, const Args& a) {
+  const float2 pa = fmul2(a.ca, xm), pb = fmul2(a.cb, x0), pc = fmul2(a.cc, xp);
+  // minus the product errors: pa - ca xm etc., exact
+  const float2 na = ffma2(a.nca, xm, pa), nb = ffma2(a.ncb, x0, pb), nc = ffma2(a.ncc, xp, pc);
+  float2 s, es, p, ep;
+  two_sum2(pa, pc, s, es);
+  two_sum2(pb, s, p, ep);
+  const float2 lo = ffma2(a.cal, xm, ffma2(a.cbl, x0, fmul2(a.ccl, xp)));
+  float2 tail = fsub2(dl, fadd2(ep, es));
+  tail = fadd2(tail, fsub2(fadd2(fadd2(na, nb), nc), lo));
+  return fadd2(fsub2(dh, p), tail);
+}
+template <bool GEN>
+R2_HD float2 res_interior(float2 dh, float2 dl, float2 xm, float2 x0, float2 xp, const Args& a) {
+  return GEN ? res_pair_gen(dh, dl, xm, x0, xp, a) : res_pair(dh, dl, xm, x0, xp, a);
 }
 // The same for one row with double-word coefficients of any value (the
 // special head and tail rows).

@@ -17,7 +17,15 @@ namespace r2 {
 // v[k] = (row k, row k + 8) of the chunk's RHS high parts in, hl the
 // system's (hi, lo) RHS pairs in the swizzled layout (xpair), and the FP64
 // results handed to store(i, row 2i, row 2i + 1, row 2i + 8, row 2i + 9).
-template <int SWEEPS, class STORE>
+// GEN: interior coefficients of any value (res_pair_gen).
+// With GEN the constants live in shared memory: a compiler fence between the
+// phases keeps their loads inside the phase that uses them (fewer registers
+// live at once).
+template <bool ON>
+__device__ __forceinline__ void phase_fence() {
+  if (ON) asm volatile("" ::: "memory");
+}
+template <int SWEEPS, bool GEN = false, class STORE>
 __device__ __forceinline__ void contiguous_solve(float2 (&v)[8], const double* hl, int j, const Args& a,
                                                  STORE store) {
   const Consts& K = a.k;
@@ -41,6 +49,7 @@ __device__ __forceinline__ void contiguous_solve(float2 (&v)[8], const double* h
       store(i, oa0, oa1, ob0, ob1);
     }
   } else {
+    phase_fence<GEN>();
     // ---- residual ----
     float xl = __shfl_up_sync(FULL, v[7].y, 1);
     float xr = __shfl_down_sync(FULL, v[0].x, 1);
@@ -75,9 +84,9 @@ __device__ __forceinline__ void contiguous_solve(float2 (&v)[8], const double* h
       const float4 qb = *reinterpret_cast<const float4*>(hl + xpair(j, i + 4));
       const int k0 = 2 * i, k1 = 2 * i + 1;
       const float2 xm0 = (k0 == 0) ? pair(xl, v[7].x) : v[k0 - 1];
-      r[k0] = res_pair(pair(qa.x, qb.x), pair(qa.y, qb.y), xm0, v[k0], v[k0 + 1], a);
+      r[k0] = res_interior<GEN>(pair(qa.x, qb.x), pair(qa.y, qb.y), xm0, v[k0], v[k0 + 1], a);
       const float2 xp1 = (k1 == 7) ? pair(v[0].y, xr) : v[k1 + 1];
-      r[k1] = res_pair(pair(qa.z, qb.z), pair(qa.w, qb.w), v[k1 - 1], v[k1], xp1, a);
+      r[k1] = res_interior<GEN>(pair(qa.z, qb.z), pair(qa.w, qb.w), v[k1 - 1], v[k1], xp1, a);
     }
     if (j == 0) {
       if (a.nh > 0) r[0].x = rsp[0];
@@ -87,6 +96,7 @@ __device__ __forceinline__ void contiguous_solve(float2 (&v)[8], const double* h
       if (a.nt > 0) r[7].y = rsp[0];
       if (a.nt > 1) r[6].y = rsp[1];
     }
+    phase_fence<GEN>();
     // ---- FP32 correction solve ----
     float CA = __shfl_up_sync(FULL, fwd_local(r, K), 1);
     if (j == 0) CA = 0.f;
@@ -96,6 +106,7 @@ __device__ __forceinline__ void contiguous_solve(float2 (&v)[8], const double* h
     bwd_fix(r, XB, K);
     if (j == 0) head_fix(r, K);
     if (j == 31) tail_fix(r, K);
+    phase_fence<GEN>();
     // ---- s (x + delta) as FP64 ----
 #pragma unroll
     for (int i = 0; i < 4; ++i) {

@@ -54,13 +54,25 @@ inline DWc to_dwc(double v) {
   return d;
 }
 
+// What prepare() accepts.  general: interior coefficients of any value
+// (the kernel then uses res_pair_gen); carry: the largest |l|^16, |w|^16
+// (the weight of the carry the 16-row chunks drop); trunc: the largest part
+// of an end correction beyond the 15 rows it is applied to.  Both limits
+// bound the FP32 solve's own error, which the refinement removes.
+struct PrepareLimits {
+  bool general = false;
+  double carry = std::ldexp(1.0, -26);
+  double trunc = std::ldexp(1.0, -25);
+};
+
 // The matrix-dependent part of Args (Consts, interior and special rows).
 // Returns false, with the reason in *why, when this solve does not apply:
-// n != 512, interior coefficients that are not powers of two, multipliers
-// that decay too slowly for the 16-row carry truncation (|l|^16 or |w|^16 >=
-// 2^-26), end corrections that reach beyond the first / last 15 rows, or an
-// ill-conditioned capacitance matrix.
-inline bool prepare(const MatrixRows& m, Args* out, std::string* why) {
+// n != 512, interior coefficients that are not powers of two (unless
+// lim.general), multipliers that decay too slowly for the 16-row carry
+// truncation (|l|^16 or |w|^16 above lim.carry), end corrections that reach
+// beyond the first / last 15 rows (lim.trunc), or an ill-conditioned
+// capacitance matrix.
+inline bool prepare(const MatrixRows& m, Args* out, std::string* why, const PrepareLimits& lim = PrepareLimits()) {
   Args a;
   std::memset(&a, 0, sizeof(a));
   auto fail = [&](const char* msg) {
@@ -70,7 +82,7 @@ inline bool prepare(const MatrixRows& m, Args* out, std::string* why) {
   const int n = m.n;
   if (n != NROWS) return fail("paired-chunk solve serves n = 512 only");
   if (m.nh < 0 || m.nh > 2 || m.nt < 0 || m.nt > 2) return fail("more than two special rows");
-  if (!pow2_or_zero(m.ai) || !pow2_or_zero(m.bi) || !pow2_or_zero(m.ci))
+  if (!lim.general && (!pow2_or_zero(m.ai) || !pow2_or_zero(m.bi) || !pow2_or_zero(m.ci)))
     return fail("interior coefficients are not powers of two");
   // pivot fixed point of the interior recurrence u = b - a c / u
   double u = m.bi;
@@ -82,8 +94,7 @@ inline bool prepare(const MatrixRows& m, Args* out, std::string* why) {
   }
   if (std::fabs(m.bi - m.ai * m.ci / u - u) > 1e-15 * std::fabs(u)) return fail("interior pivots do not converge");
   const double l = m.ai / u, w = m.ci / u, g = 1.0 / u;
-  const double lim = std::ldexp(1.0, -26);
-  if (std::pow(std::fabs(l), 16) > lim || std::pow(std::fabs(w), 16) > lim)
+  if (std::pow(std::fabs(l), 16) > lim.carry || std::pow(std::fabs(w), 16) > lim.carry)
     return fail("multipliers decay too slowly for 16-row carries");
   Consts& k = a.k;
   k.nl = splat((float)-l);
@@ -172,7 +183,7 @@ inline bool prepare(const MatrixRows& m, Args* out, std::string* why) {
   double Rh[2][2] = {{0}}, Rt[2][2] = {{0}};
   if (!inv(Ch, nh, Rh) || !inv(Ct, nt, Rt)) return fail("end correction is ill-conditioned");
   // P_j = sum_i p_i (C_h^-1)_ij over rows 0..15; row 15 must be negligible
-  const double trunc = std::ldexp(1.0, -25);
+  const double trunc = lim.trunc;
   k.nh = nh;
   k.nt = nt;
   for (int jj = 0; jj < nh; ++jj) {
@@ -210,6 +221,12 @@ inline bool prepare(const MatrixRows& m, Args* out, std::string* why) {
   a.ca = splat((float)m.ai);
   a.cb = splat((float)m.bi);
   a.cc = splat((float)m.ci);
+  a.cal = splat(to_dwc(m.ai).l);
+  a.cbl = splat(to_dwc(m.bi).l);
+  a.ccl = splat(to_dwc(m.ci).l);
+  a.nca = splat(-(float)m.ai);
+  a.ncb = splat(-(float)m.bi);
+  a.ncc = splat(-(float)m.ci);
   a.nh = m.nh;
   a.nt = m.nt;
   for (int i = 0; i < 2; ++i) {

@@ -378,6 +378,13 @@ class UnevenBatch:
         check(load().ntk_batch_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         return {"max_n": a.value, "segmented": b.value, "elements": c.value}
 
+    def windows(self):
+        """{"windows": 512-row windows solved, "paired": how many of them on
+        the paired-chunk FP32 solve (FP32 / FP32 + refinement batches).}"""
+        w, p = ctypes.c_longlong(), ctypes.c_longlong()
+        check(load().ntk_batch_windows(self._h, ctypes.byref(w), ctypes.byref(p)))
+        return {"windows": w.value, "paired": p.value}
+
     def solve(self, d, stream=None):
         ne = _available(d)
         if ne is not None and ne < self.elements:

@@ -74,6 +74,7 @@ SIGNATURES = [
     ("ntk_batch_destroy", _i, [_vp]),
     ("ntk_batch_status", _i, [_vp, ctypes.POINTER(_i), _vp]),
     ("ntk_batch_info", _i, [_vp, ctypes.POINTER(_ll), ctypes.POINTER(_ll), ctypes.POINTER(_ll)]),
+    ("ntk_batch_windows", _i, [_vp, ctypes.POINTER(_ll), ctypes.POINTER(_ll)]),
     ("ntk_batch_solve", _i, [_vp, _vp, _vp]),
 ]
 

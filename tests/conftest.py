@@ -79,6 +79,8 @@ def r2emu(tmp_path_factory):
     d = ctypes.c_double
     lib.r2emu_solve.argtypes = [ctypes.c_int, ctypes.c_int, P(d), P(d), d, d, d, ctypes.c_int, d, ctypes.c_int,
                                 ctypes.c_longlong, P(d), P(d), ctypes.c_char_p, ctypes.c_int]
+    lib.r2emu_solve_general.argtypes = [ctypes.c_int, ctypes.c_int, P(d), P(d), d, d, d, d, d, ctypes.c_int,
+                                        ctypes.c_longlong, P(d), P(d), ctypes.c_char_p, ctypes.c_int]
     lib.r2emu_split.argtypes = [P(d), ctypes.c_longlong, P(ctypes.c_float), P(ctypes.c_float)]
     lib.r2emu_dw.argtypes = [P(ctypes.c_float), P(ctypes.c_float), ctypes.c_longlong, P(d)]
     return lib

@@ -14,7 +14,7 @@ using namespace ntk::r2;
 namespace {
 
 void emulate_system(const Args& a, bool compact, int sweeps, const double* f, double* out, unsigned* rmax_out,
-                    int* edge_mismatch) {
+                    int* edge_mismatch, bool gen = false) {
   const Consts& K = a.k;
   float2 v[CHUNKS][8], dh[CHUNKS][8], dl[CHUNKS][8];
   unsigned rmax = 0;
@@ -69,7 +69,7 @@ void emulate_system(const Args& a, bool compact, int sweeps, const double* f, do
     for (int k = 0; k < HALF; ++k) {
       const float2 xm = k == 0 ? pair(xl, x[HALF - 1].x) : x[k - 1];
       const float2 xp = k == HALF - 1 ? pair(x[0].y, xr) : x[k + 1];
-      r[c][k] = res_pair(dh[c][k], dl[c][k], xm, x[k], xp, a);
+      r[c][k] = gen ? res_pair_gen(dh[c][k], dl[c][k], xm, x[k], xp, a) : res_pair(dh[c][k], dl[c][k], xm, x[k], xp, a);
     }
   }
   {
@@ -143,6 +143,45 @@ int r2emu_solve(int nh, int nt, const double* head, const double* tail, double a
   for (long long s = 0; s < nsys; ++s) {
     unsigned r = 0;
     emulate_system(a, compact != 0, sweeps, f + s * NROWS, out + s * NROWS, &r, &mism);
+    rmax = umax(rmax, r);
+  }
+  if (mism) return 3;
+  return rmax >= (1151u << 20) ? 2 : 0;
+}
+
+// The same solve (d = f in place) for interior coefficients of any value
+// (prepare with PrepareLimits::general and the given truncation limits; the
+// residual res_pair_gen), as the uneven-batch windows run it.
+int r2emu_solve_general(int nh, int nt, const double* head, const double* tail, double ai, double bi, double ci,
+                        double carry, double trunc, int sweeps, long long nsys, const double* f, double* out,
+                        char* why, int whylen) {
+  MatrixRows m;
+  m.n = NROWS;
+  m.nh = nh;
+  m.nt = nt;
+  for (int i = 0; i < 2; ++i)
+    for (int q = 0; q < 3; ++q) {
+      m.head[i][q] = head[3 * i + q];
+      m.tail[i][q] = tail[3 * i + q];
+    }
+  m.ai = ai;
+  m.bi = bi;
+  m.ci = ci;
+  PrepareLimits lim;
+  lim.general = true;
+  lim.carry = carry;
+  lim.trunc = trunc;
+  Args a;
+  std::string w;
+  if (!prepare(m, &a, &w, lim)) {
+    if (why && whylen > 0) std::snprintf(why, whylen, "%s", w.c_str());
+    return 1;
+  }
+  unsigned rmax = 0;
+  int mism = 0;
+  for (long long s = 0; s < nsys; ++s) {
+    unsigned r = 0;
+    emulate_system(a, false, sweeps, f + s * NROWS, out + s * NROWS, &r, &mism, true);
     rmax = umax(rmax, r);
   }
   if (mism) return 3;

@@ -207,3 +207,44 @@ def test_repeated_solves_in_one_stream(cuda, oracle, precision, tol):
             a, b, c = _bands(int(n), interior[s], head[s], tail[s])
             ref = oracle.thomas_ld(a, b, c, d[o:o + n])
             assert oracle.rel_err(x[o:o + n], ref) < tol, (s, n)
+
+
+def test_refine_benchmark_batch_takes_the_paired_chunk_windows(cuda):
+    """The 4096-system batch (a, c <= 0.3): every 512-row window of the long
+    systems qualifies for the paired-chunk solve (constant Toeplitz factors,
+    end corrections per window kind)."""
+    import ntk
+    from ntk.workloads import uneven_batch
+
+    lengths, systems = uneven_batch(4096, seed=0)
+    interior, head, tail = _descriptors(lengths, systems)
+    with ntk.UnevenBatch(lengths, interior, head, tail, precision="fp32_refine") as bt:
+        w = bt.windows()
+    short = int(np.sum(np.asarray(lengths) < 512))
+    assert w["paired"] == w["windows"] - short, w
+
+
+@pytest.mark.parametrize("precision,tol", [("fp32_refine", REFINE_TOL), ("fp32", 2e-5)])
+def test_mixed_paired_and_chunked_windows(cuda, oracle, precision, tol):
+    """Systems whose factors decay fast (a = c = 0.2: paired-chunk windows)
+    beside systems that decay slowly (a = c = 0.45: the chunked windows with
+    per-window tables) and short ones, at unaligned offsets, in one launch."""
+    import ntk
+
+    lengths = np.array([512, 1500, 3000, 700, 512, 2048, 300, 4099])
+    k = len(lengths)
+    slow = np.array([0, 1, 0, 1, 1, 0, 0, 1], bool)
+    ac = np.where(slow, 0.45, 0.2)
+    interior = np.column_stack([ac, np.ones(k), ac])
+    rng = np.random.default_rng(21)
+    head = rng.uniform(-0.3, 0.3, size=(k, 2, 3))
+    head[:, :, 1] = 1.8
+    tail = rng.uniform(-0.3, 0.3, size=(k, 2, 3))
+    tail[:, :, 1] = 1.8
+    offsets = np.cumsum(np.concatenate([[3], lengths[:-1] + 1]))
+    with ntk.UnevenBatch(lengths, interior, head, tail, offsets=offsets, precision=precision) as bt:
+        w = bt.windows()
+    assert 0 < w["paired"] < w["windows"], w
+    worst, _, _, _ = _check(cuda, oracle, lengths, interior, head, tail, seed=22, offsets=offsets,
+                            precision=precision)
+    assert worst < tol, worst

@@ -113,3 +113,61 @@ def test_split_and_assembly(r2emu):
     r2emu.r2emu_dw(s.ctypes.data_as(F), e.ctypes.data_as(F), m, out.ctypes.data_as(D))
     exact = h.astype(np.float64) + d.astype(np.float64)
     assert np.max(np.abs(out - exact) / np.abs(exact)) <= 2.0 ** -47 * (1 + 2.0 ** -20)
+
+
+def _window_rows(kind, abc, head6, tail6):
+    """Bands of one 512-row window of an uneven-batch system (ntk_batch_refine.cu):
+    kind 'first' (the system's head rows, the tail cut), 'middle' (both cut:
+    row 0 = (0, b, c), the last row (a, b, 0)), 'last' (head cut, the
+    system's tail rows) or 'whole'."""
+    ai, bi, ci = abc
+    a = np.full(N, ai)
+    b = np.full(N, bi)
+    c = np.full(N, ci)
+    if kind in ("first", "whole"):
+        a[0], b[0], c[0] = 0., head6[1], head6[2]
+        a[1], b[1], c[1] = head6[3:6]
+        nh, head = 2, [0., head6[1], head6[2]] + list(head6[3:6])
+    else:
+        nh, head = 1, [0., bi, ci, 0., 1., 0.]
+    if kind in ("last", "whole"):
+        a[-2], b[-2], c[-2] = tail6[0:3]
+        a[-1], b[-1] = tail6[3], tail6[4]
+        nt, tail = 2, list(tail6[0:5]) + [0.]
+    else:
+        nt, tail = 0, [0., 1., 0., 0., 1., 0.]
+    a[0] = c[-1] = 0.
+    return (a, b, c), nh, nt, head, tail
+
+
+@pytest.mark.parametrize("kind", ["first", "middle", "last", "whole"])
+def test_general_coefficient_windows_match_long_double_thomas(r2emu, oracle, kind):
+    """The uneven batch's paired-chunk windows: interior coefficients of any
+    value (a, c up to 0.3, b = 1, the benchmark batch's range, and the
+    slowest decay it has), random diagonally dominant end rows, one sweep
+    within the refinement tolerance of a long-double solve."""
+    import ctypes
+
+    P = ctypes.POINTER(ctypes.c_double)
+    rng = np.random.default_rng(11)
+    for ai, ci in ((0.1, 0.1), (0.3, 0.3), (0.137, 0.291)):
+        h = []
+        for _ in range(2):
+            aa, cc = rng.uniform(-0.4, 0.4, size=2)
+            h += [aa, abs(aa) + abs(cc) + rng.uniform(0.5, 1.5), cc]
+        t = []
+        for _ in range(2):
+            aa, cc = rng.uniform(-0.4, 0.4, size=2)
+            t += [aa, abs(aa) + abs(cc) + rng.uniform(0.5, 1.5), cc]
+        (a, b, c), nh, nt, head, tail = _window_rows(kind, (ai, 1.0, ci), h, t)
+        d = rng.normal(size=(8, N))
+        out = np.zeros_like(d)
+        hd = np.ascontiguousarray(head, dtype=np.float64)
+        tl = np.ascontiguousarray(tail, dtype=np.float64)
+        why = ctypes.create_string_buffer(256)
+        rc = r2emu.r2emu_solve_general(nh, nt, hd.ctypes.data_as(P), tl.ctypes.data_as(P), ai, 1.0, ci,
+                                       2.0 ** -22, 2.0 ** -22, 1, d.shape[0], d.ctypes.data_as(P),
+                                       out.ctypes.data_as(P), why, 256)
+        assert rc == 0, why.value
+        ref = np.array([oracle.thomas_ld(a, b, c, row) for row in d])
+        assert oracle.rel_err(out, ref) < 1e-13, (kind, ai, ci)
