@@ -53,13 +53,18 @@ struct BatchWin {
   int sysi = 0;                // the system's counter
   int wfirst = 0, wcount = 1;  // the system's windows
   int args = -1;               // paired-chunk windows: index of the kind's constants
+  int ccount = 0;              // paired-chunk windows: the system's windows in this window's CTA
+                               // when it is the first of them there, else 0
 };
 
 namespace refine_detail {
 
 constexpr int BM = 16;                  // rows per lane
 constexpr int BLW = 32 * BM;            // window rows
-constexpr int BW = 4;                   // warps (windows) per CTA
+#ifndef NTK_BATCH_BW
+#define NTK_BATCH_BW 4
+#endif
+constexpr int BW = NTK_BATCH_BW;        // warps (windows) per CTA (a build flag, for tuning experiments)
 // Table slots of one warp: lanes whose chunks (and the three rows before
 // them) see the same coefficients build identical tables, so they share a
 // slot: 0 lane 0 (the window's head), 1 interior lanes, 2..4 the lanes
@@ -270,14 +275,15 @@ __device__ __noinline__ void refine_window_call(double* work, double* dst, const
 // batch and copied into shared memory), interior coefficients of any value
 // in the residual.  The warp stages its 512 rows with 8-byte copies into a
 // 4 KB tile in the 128-byte-swizzled layout the solve reads (rows 2i, 2i + 1
-// of chunk j at xpair(j, i)), rewrites them as (hi, lo) pairs, solves, puts
-// the results back into the tile and stores the window's central rows with
-// coalesced stores (border rows to work, as in refine_window).
-template <int SWEEPS>
-__device__ __forceinline__ void r2_window(double* work, double* dst, const BatchWin* __restrict__ wins,
-                                          const r2::Args* __restrict__ args, long long item, unsigned* status,
-                                          unsigned* done, r2::Args* sa, double* tile, unsigned lane) {
-  const BatchWin* wp = wins + item;
+// of chunk j at xpair(j, i)); after a CTA barrier (every window of the CTA
+// has read its rows) it rewrites them as (hi, lo) pairs, solves, puts the
+// results back into the tile and stores the window's central rows with
+// coalesced stores.  Neighbouring windows in the same CTA have read their
+// rows before the barrier, so only rows that a window in another CTA reads
+// (border rows) go to the work array.
+__device__ __forceinline__ void r2_stage(const double* d, const BatchWin* __restrict__ wp,
+                                         const r2::Args* __restrict__ args, r2::Args* sa, double* tile,
+                                         unsigned lane) {
   const long long off = __ldg(&wp->off);
   {
     const unsigned long long* g = reinterpret_cast<const unsigned long long*>(args + __ldg(&wp->args));
@@ -285,16 +291,17 @@ __device__ __forceinline__ void r2_window(double* work, double* dst, const Batch
     constexpr int NA = (int)(sizeof(r2::Args) / sizeof(unsigned long long));
     for (int i = (int)lane; i < NA; i += 32) sd[i] = __ldg(g + i);
   }
-  {
-    const double* src = dst + off;
+  const double* src = d + off;
 #pragma unroll
-    for (int q = 0; q < BM; ++q) {
-      const int r = (int)lane + 32 * q;
-      cp_async8(tile + r2::xpair(r >> 4, (r & 15) >> 1) + (r & 1), src + r, 8u);
-    }
+  for (int q = 0; q < BM; ++q) {
+    const int r = (int)lane + 32 * q;
+    cp_async8(tile + r2::xpair(r >> 4, (r & 15) >> 1) + (r & 1), src + r, 8u);
   }
-  cp_async_wait_all();
-  __syncwarp();
+}
+
+template <int SWEEPS>
+__device__ __forceinline__ void r2_solve(double* work, double* dst, const BatchWin* __restrict__ wp,
+                                         unsigned* status, const r2::Args* sa, double* tile, unsigned lane) {
   const int j = (int)lane;
   unsigned rmax = 0;
   float2 v[8];
@@ -319,6 +326,7 @@ __device__ __forceinline__ void r2_window(double* work, double* dst, const Batch
   });
   __syncwarp();
   {
+    const long long off = __ldg(&wp->off);
     const int lo = __ldg(&wp->out_lo), hi = __ldg(&wp->out_hi);
     const int blo = __ldg(&wp->blo), bhi = __ldg(&wp->bhi);
 #pragma unroll 4
@@ -329,13 +337,35 @@ __device__ __forceinline__ void r2_window(double* work, double* dst, const Batch
     }
   }
   if (__any_sync(0xffffffffu, rmax >= r2::RANGE_MAG) && lane == 0 && status) atomicOr(status, 1u);
-  if (__ldg(&wp->wcount) > 1) {
-    BatchWin w;
-    w.sysi = __ldg(&wp->sysi);
-    w.wfirst = __ldg(&wp->wfirst);
-    w.wcount = __ldg(&wp->wcount);
-    finish_system(work, dst, wins, w, done, lane);
+}
+
+// After a CTA barrier that follows every window's stores: the first window
+// in this CTA of a system that other CTAs share adds the CTA's windows of
+// that system to the system's counter; the warp that completes the count
+// copies the system's border rows from work into d and resets the counter.
+__device__ __forceinline__ void r2_finish(const double* work, double* dst, const BatchWin* __restrict__ wins,
+                                          const BatchWin* __restrict__ wp, unsigned* done, unsigned lane) {
+  const int cc = __ldg(&wp->ccount);
+  const int wcount = __ldg(&wp->wcount);
+  if (cc == 0 || cc == wcount) return;  // not the first here, or the whole system is in this CTA
+  const int sysi = __ldg(&wp->sysi);
+  unsigned last = 0;
+  if (lane == 0) {
+    __threadfence();
+    last = atomicAdd(done + sysi, (unsigned)cc) == (unsigned)(wcount - cc);
+    if (last) __threadfence();
   }
+  if (!__shfl_sync(0xffffffffu, last, 0)) return;
+  border_copy(work, dst, __ldg(&wp->wfirst), wcount, lane,
+              [&](int g, long long& base, int& lo, int& blo, int& bhi, int& hi) {
+                const BatchWin* v = wins + g;
+                base = __ldg(&v->off);
+                lo = __ldg(&v->out_lo);
+                hi = __ldg(&v->out_hi);
+                blo = min(__ldg(&v->blo), hi);
+                bhi = max(__ldg(&v->bhi), lo);
+              });
+  if (lane == 0) done[sysi] = 0u;
 }
 
 // L2 prefetch of window `item`'s rows (issued by one lane): the window the
@@ -386,9 +416,11 @@ constexpr size_t R2_ARGS_BYTES = (sizeof(r2::Args) + 15) / 16 * 16;
 constexpr size_t r2_smem() { return (size_t)BW * NROWS_R2 * sizeof(double) + (size_t)BW * R2_ARGS_BYTES; }
 
 // CTAs per SM the kernel is compiled for (registers per thread: 65536 /
-// (32 BW x this)); a build flag, for tuning experiments.
+// (32 BW x this)); a build flag, for tuning experiments.  Five (96
+// registers) measured 0.068 ms for the 4096-system batch against 0.069-0.070
+// with six (80 registers, more spilled) and 0.089 with one 16-warp CTA.
 #ifndef NTK_BATCH_MINB
-#define NTK_BATCH_MINB 6
+#define NTK_BATCH_MINB 5
 #endif
 
 // The whole batch in one launch.  Each warp first prefetches into L2 the
@@ -409,14 +441,20 @@ __global__ void __launch_bounds__(32 * BW, NTK_BATCH_MINB)
   }
   int kind;
   const long long it = window_of(blockIdx.x, warp, g, kind);
-  if (it < 0) return;
-  if (kind == 0) {
+  if (kind == 0) {  // the whole CTA: every thread reaches both barriers
     double* tile = reinterpret_cast<double*>(smem_raw) + (size_t)warp * NROWS_R2;
     r2::Args* sa = reinterpret_cast<r2::Args*>(smem_raw + (size_t)BW * NROWS_R2 * sizeof(double) +
                                                (size_t)warp * R2_ARGS_BYTES);
-    r2_window<SWEEPS>(work, d, wins, args, it, status, done, sa, tile, lane);
+    const BatchWin* wp = wins + (it >= 0 ? it : 0);
+    if (it >= 0) r2_stage(d, wp, args, sa, tile, lane);
+    cp_async_wait_all();
+    __syncthreads();  // every window of the CTA has read its rows from d
+    if (it >= 0) r2_solve<SWEEPS>(work, d, wp, status, sa, tile, lane);
+    __syncthreads();  // every window of the CTA has stored its rows
+    if (it >= 0) r2_finish(work, d, wins, wp, done, lane);
     return;
   }
+  if (it < 0) return;
   float4* tq = reinterpret_cast<float4*>(smem_raw) + (size_t)warp * BTAB;
   BatchWin* wa = reinterpret_cast<BatchWin*>(reinterpret_cast<float4*>(smem_raw) + (size_t)BW * BTAB) + warp;
   double* trow = reinterpret_cast<double*>(reinterpret_cast<BatchWin*>(reinterpret_cast<float4*>(smem_raw) +
@@ -685,6 +723,36 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
     }
   }
   for (BatchWin& w : full) w.wfirst += (int)r2w.size();
+  // Paired-chunk windows run BW to a CTA (consecutive in r2w) and every
+  // window of a CTA reads its rows before any of them stores, so only the
+  // rows a window in another CTA reads are border rows: those below the end
+  // of the last earlier window of the system in another CTA and those from
+  // the start of the first later one on (the windows' row ranges increase
+  // with their index, so these two bound every other CTA's reads; the last
+  // window can reach back past its neighbour into the window before).  The
+  // first window of a system in each CTA counts that CTA's windows of it.
+  for (size_t i = 0; i < r2w.size(); ++i) {
+    BatchWin& w = r2w[i];
+    const size_t first = (size_t)w.wfirst, last = first + (size_t)w.wcount - 1;
+    const size_t cta = i / BW;
+    const size_t cta_lo = cta * BW, cta_hi = cta_lo + BW - 1;  // this CTA's windows
+    w.blo = w.out_lo;
+    w.bhi = w.out_hi;
+    if (cta_lo > first) {  // window cta_lo - 1: the system's last window in an earlier CTA
+      const long long end = r2w[cta_lo - 1].off + BLW - w.off;
+      w.blo = (int)std::min<long long>(w.out_hi, std::max<long long>(w.out_lo, end));
+    }
+    if (cta_hi < last) {  // window cta_hi + 1: the system's first window in a later CTA
+      const long long start = r2w[cta_hi + 1].off - w.off;
+      w.bhi = (int)std::max<long long>(w.out_lo, std::min<long long>(w.out_hi, start));
+    }
+    w.ccount = 0;
+    if (i == first || (i - 1) / BW != cta) {
+      size_t e = i;
+      while (e < last && (e + 1) / BW == cta) ++e;
+      w.ccount = (int)(e - i + 1);
+    }
+  }
   BatchRefine* br = new (std::nothrow) BatchRefine();
   if (!br) {
     set_error("out of host memory");
