@@ -55,6 +55,7 @@ struct BatchWin {
   int args = -1;               // paired-chunk windows: index of the kind's constants
   int ccount = 0;              // paired-chunk windows: the system's windows in this window's CTA
                                // when it is the first of them there, else 0
+  int rfirst = 0, rcount = 0;  // paired-chunk windows: the system's border rows in the row list
 };
 
 namespace refine_detail {
@@ -341,31 +342,39 @@ __device__ __forceinline__ void r2_solve(double* work, double* dst, const BatchW
 
 // After a CTA barrier that follows every window's stores: the first window
 // in this CTA of a system that other CTAs share adds the CTA's windows of
-// that system to the system's counter; the warp that completes the count
-// copies the system's border rows from work into d and resets the counter.
-__device__ __forceinline__ void r2_finish(const double* work, double* dst, const BatchWin* __restrict__ wins,
-                                          const BatchWin* __restrict__ wp, unsigned* done, unsigned lane) {
+// that system to the system's counter.  Returns true (warp-uniform) in the
+// warp that completes the count: every window of the system has stored.
+__device__ __forceinline__ bool r2_count(const BatchWin* __restrict__ wp, unsigned* done, unsigned lane) {
   const int cc = __ldg(&wp->ccount);
   const int wcount = __ldg(&wp->wcount);
-  if (cc == 0 || cc == wcount) return;  // not the first here, or the whole system is in this CTA
-  const int sysi = __ldg(&wp->sysi);
+  if (cc == 0 || cc == wcount) return false;  // not the first here, or the whole system is in this CTA
   unsigned last = 0;
   if (lane == 0) {
     __threadfence();
-    last = atomicAdd(done + sysi, (unsigned)cc) == (unsigned)(wcount - cc);
+    last = atomicAdd(done + __ldg(&wp->sysi), (unsigned)cc) == (unsigned)(wcount - cc);
     if (last) __threadfence();
   }
-  if (!__shfl_sync(0xffffffffu, last, 0)) return;
-  border_copy(work, dst, __ldg(&wp->wfirst), wcount, lane,
-              [&](int g, long long& base, int& lo, int& blo, int& bhi, int& hi) {
-                const BatchWin* v = wins + g;
-                base = __ldg(&v->off);
-                lo = __ldg(&v->out_lo);
-                hi = __ldg(&v->out_hi);
-                blo = min(__ldg(&v->blo), hi);
-                bhi = max(__ldg(&v->bhi), lo);
-              });
-  if (lane == 0) done[sysi] = 0u;
+  return __shfl_sync(0xffffffffu, last, 0) != 0;
+}
+
+// The CTA's threads copy a system's border rows (absolute row indices in
+// rows[0, count)) from work into d, eight rows a thread in flight.
+__device__ __forceinline__ void row_copy(const double* work, double* d, const long long* __restrict__ rows,
+                                         int count, int t, int nt) {
+  for (int base = 0; base < count; base += 8 * nt) {
+    long long at[8];
+    double v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int i = base + t + q * nt;
+      at[q] = i < count ? __ldg(rows + i) : -1;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = at[q] >= 0 ? __ldcg(work + at[q]) : 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (at[q] >= 0) d[at[q]] = v[q];
+  }
 }
 
 // L2 prefetch of window `item`'s rows (issued by one lane): the window the
@@ -428,8 +437,8 @@ constexpr size_t r2_smem() { return (size_t)BW * NROWS_R2 * sizeof(double) + (si
 template <int SWEEPS>
 __global__ void __launch_bounds__(32 * BW, NTK_BATCH_MINB)
     batch_refine_kernel(double* work, double* d, const BatchWin* __restrict__ wins,
-                        const r2::Args* __restrict__ args, unsigned* status, unsigned* done,
-                        const __grid_constant__ BatchGeo g) {
+                        const r2::Args* __restrict__ args, const long long* __restrict__ border_rows,
+                        unsigned* status, unsigned* done, const __grid_constant__ BatchGeo g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int P = sys_pitch<BM>();
   const int warp = threadIdx.x >> 5;
@@ -445,13 +454,25 @@ __global__ void __launch_bounds__(32 * BW, NTK_BATCH_MINB)
     double* tile = reinterpret_cast<double*>(smem_raw) + (size_t)warp * NROWS_R2;
     r2::Args* sa = reinterpret_cast<r2::Args*>(smem_raw + (size_t)BW * NROWS_R2 * sizeof(double) +
                                                (size_t)warp * R2_ARGS_BYTES);
+    __shared__ int last_win[BW];  // windows whose warp completed their system's count
     const BatchWin* wp = wins + (it >= 0 ? it : 0);
     if (it >= 0) r2_stage(d, wp, args, sa, tile, lane);
     cp_async_wait_all();
     __syncthreads();  // every window of the CTA has read its rows from d
     if (it >= 0) r2_solve<SWEEPS>(work, d, wp, status, sa, tile, lane);
     __syncthreads();  // every window of the CTA has stored its rows
-    if (it >= 0) r2_finish(work, d, wins, wp, done, lane);
+    const bool last = it >= 0 && r2_count(wp, done, lane);
+    if (lane == 0) last_win[warp] = last ? (int)it : -1;
+    __syncthreads();
+    // the systems this CTA completed: every window of theirs has stored, so
+    // their border rows go from work into d (by then nothing reads them)
+    for (int k = 0; k < BW; ++k) {
+      const int wi = last_win[k];
+      if (wi < 0) continue;
+      const BatchWin* lw = wins + wi;
+      row_copy(work, d, border_rows + __ldg(&lw->rfirst), __ldg(&lw->rcount), (int)threadIdx.x, 32 * BW);
+      if (threadIdx.x == 0) done[__ldg(&lw->sysi)] = 0u;
+    }
     return;
   }
   if (it < 0) return;
@@ -479,11 +500,13 @@ struct BatchRefine {
   unsigned ctas = 0;
   BatchWin* d_wins = nullptr;
   r2::Args* d_args = nullptr;  // the paired-chunk window kinds' constants
+  long long* d_rows = nullptr;  // the paired-chunk windows' border rows, grouped by system
   unsigned* d_status = nullptr;
   unsigned* d_done = nullptr;  // per system: its windows finished in the current launch
   ~BatchRefine() {
     if (d_wins) cudaFree(d_wins);
     if (d_args) cudaFree(d_args);
+    if (d_rows) cudaFree(d_rows);
     if (d_status) cudaFree(d_status);
     if (d_done) cudaFree(d_done);
   }
@@ -753,6 +776,23 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
       w.ccount = (int)(e - i + 1);
     }
   }
+  // each system's border rows (absolute indices), for the CTA that
+  // completes the system's count
+  std::vector<long long> rows;
+  for (size_t i = 0; i < r2w.size();) {
+    const size_t first = i, end = i + (size_t)r2w[i].wcount;
+    const int rf = (int)rows.size();
+    for (size_t k = first; k < end; ++k) {
+      const BatchWin& w = r2w[k];
+      for (int r = w.out_lo; r < w.blo; ++r) rows.push_back(w.off + r);
+      for (int r = w.bhi; r < w.out_hi; ++r) rows.push_back(w.off + r);
+    }
+    for (size_t k = first; k < end; ++k) {
+      r2w[k].rfirst = rf;
+      r2w[k].rcount = (int)rows.size() - rf;
+    }
+    i = end;
+  }
   BatchRefine* br = new (std::nothrow) BatchRefine();
   if (!br) {
     set_error("out of host memory");
@@ -782,6 +822,12 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
       rc = cuda_status(
           cudaMemcpy(br->d_args, r2args.data(), sizeof(r2::Args) * r2args.size(), cudaMemcpyHostToDevice),
           "cudaMemcpy(window constants)");
+  }
+  if (!rc && !rows.empty()) {
+    rc = cuda_status(cudaMalloc(&br->d_rows, sizeof(long long) * rows.size()), "cudaMalloc(border rows)");
+    if (!rc)
+      rc = cuda_status(cudaMemcpy(br->d_rows, rows.data(), sizeof(long long) * rows.size(), cudaMemcpyHostToDevice),
+                       "cudaMemcpy(border rows)");
   }
   if (!rc) rc = cuda_status(cudaMalloc(&br->d_status, sizeof(unsigned)), "cudaMalloc(status)");
   if (!rc) rc = cuda_status(cudaMemset(br->d_status, 0, sizeof(unsigned)), "cudaMemset(status)");
@@ -819,7 +865,8 @@ int batch_refine_solve(BatchRefine* br, double* d, double* work, cudaStream_t st
   using namespace refine_detail;
   if (br->ctas == 0) return NTK_OK;
   auto kern = br->sweeps == 0 ? batch_refine_kernel<0> : batch_refine_kernel<1>;
-  kern<<<br->ctas, 32 * BW, batch_smem(), st>>>(work, d, br->d_wins, br->d_args, br->d_status, br->d_done, br->geo);
+  kern<<<br->ctas, 32 * BW, batch_smem(), st>>>(work, d, br->d_wins, br->d_args, br->d_rows, br->d_status,
+                                                br->d_done, br->geo);
   return cuda_status(cudaGetLastError(), "batch_refine_kernel");
 }
 
