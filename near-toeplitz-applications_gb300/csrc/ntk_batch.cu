@@ -33,6 +33,7 @@
 #include <numeric>
 #include <vector>
 
+#include "ntk_batch_borders.h"
 #include "ntk_batch_refine.h"
 #include "ntk_device.cuh"
 #include "ntk_internal.h"
@@ -64,6 +65,8 @@ struct F64Win {
   // reads them): written to work during the solve, copied into d at the end
   int blo, bhi;
   int sysi, wfirst, wcount;  // the system's counter and windows
+  int ccount;                // the system's windows in this window's CTA when it is the first there, else 0
+  int rfirst, rcount;        // the system's border rows in the row list (ntk_batch_borders.h)
 };
 
 namespace {
@@ -166,22 +169,27 @@ __device__ __forceinline__ void f64w_fac(const F64Win& w, const double* __restri
   if (r == F64W_LW - 1 && i < w.n - 1) c = 0.0;  // cut end
 }
 
-// Window wi by one warp: all rows read from d, the central rows written to d
-// except the border rows, which go to work.
+// Window wi by one warp, in two parts around a CTA barrier: its rows staged
+// from d (coalesced; padding rows zero-filled), then solved and its central
+// rows written to d except the border rows, which go to work.
+__device__ __forceinline__ void f64_stage(const double* d, const F64Win* __restrict__ wins, long long wi,
+                                         double* tile, int lane) {
+  constexpr int M = F64W_M;
+  const long long base = __ldg(&wins[wi].off) + __ldg(&wins[wi].w0);
+  const int rows = __ldg(&wins[wi].n) - __ldg(&wins[wi].w0);
+#pragma unroll
+  for (int q = 0; q < M; ++q) {
+    const int r = lane + 32 * q;
+    const bool ok = r < rows;
+    cp_async8(tile + (r / M) * (M + 1) + (r % M), ok ? d + base + r : d, ok ? 8u : 0u);
+  }
+}
+
 __device__ __forceinline__ void f64_window(double* work, double* d, const F64Win* __restrict__ wins,
                                         long long wi, const double* __restrict__ pool, double* tile, int lane) {
   constexpr int M = F64W_M;
   constexpr unsigned FULL = 0xffffffffu;
   const F64Win w = wins[wi];
-  // stage rows (coalesced); padding rows are zero-filled
-#pragma unroll
-  for (int q = 0; q < M; ++q) {
-    const int r = lane + 32 * q;
-    const bool ok = w.w0 + r < w.n;
-    cp_async8(tile + (r / M) * (M + 1) + (r % M), ok ? d + w.off + w.w0 + r : d, ok ? 8u : 0u);
-  }
-  cp_async_wait_all();
-  __syncwarp();
   const int r0 = lane * M;
   double v[M];
 #pragma unroll
@@ -267,19 +275,22 @@ __device__ __forceinline__ void f64_window(double* work, double* d, const F64Win
 }
 
 // All windows in one launch, in place, without a copy of the whole buffer
-// and without waiting: every window reads its rows from d and writes its
-// central rows to d except its border rows (central rows a neighbouring
-// window reads), which go to work, so d keeps every halo row unchanged while
-// the system's windows run; each window of a multi-window system then counts
-// itself done on the system's counter, and the window that finishes last
-// copies the system's border rows from work into d and resets the counter.
-// Each warp first prefetches into L2 the window of the warp pf CTAs further
-// on (pf = the CTAs resident at once), so that window's staging finds it in
-// L2.
+// and without waiting: a CTA's four windows stage their rows, a CTA barrier,
+// then each solves and writes its central rows to d except its border rows
+// (central rows a window in another CTA reads, ntk_batch_borders.h), which
+// go to work, so d keeps every row another CTA reads unchanged while the
+// system's windows run.  After a second barrier the first window of a
+// system in the CTA adds the CTA's windows of it to the system's counter;
+// the CTA that completes the count copies the system's border rows from work
+// into d with all its threads and resets the counter.  Each warp first
+// prefetches into L2 the window of the warp pf CTAs further on (pf = the
+// CTAs resident at once), so that window's staging finds it in L2.
 __global__ void __launch_bounds__(128, 5) batch_f64w_kernel(double* work, double* d, const F64Win* __restrict__ wins,
                                                             long long nwin, const double* __restrict__ pool,
+                                                            const long long* __restrict__ border_rows,
                                                             unsigned* done, unsigned pf) {
   __shared__ __align__(16) double tiles[F64W_WARPS * F64W_PITCH];
+  __shared__ int last_win[F64W_WARPS];
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const long long wi = (long long)blockIdx.x * F64W_WARPS + warp;
@@ -291,29 +302,35 @@ __global__ void __launch_bounds__(128, 5) batch_f64w_kernel(double* work, double
     const uintptr_t e = (reinterpret_cast<uintptr_t>(d + base + rows) + 15) & ~(uintptr_t)15;
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)(e - a)) : "memory");
   }
-  if (wi >= nwin) return;  // whole warps leave; no CTA barrier follows
-  f64_window(work, d, wins, wi, pool, tiles + warp * F64W_PITCH, lane);
-  const int wcount = __ldg(&wins[wi].wcount);
-  if (wcount < 2) return;
-  __syncwarp();
-  unsigned last = 0;
-  const int sysi = __ldg(&wins[wi].sysi);
-  if (lane == 0) {
-    __threadfence();
-    last = atomicAdd(done + sysi, 1u) == (unsigned)wcount - 1;
-    if (last) __threadfence();
+  const bool live = wi < nwin;  // every thread reaches the barriers
+  double* tile = tiles + warp * F64W_PITCH;
+  if (live) f64_stage(d, wins, wi, tile, lane);
+  cp_async_wait_all();
+  __syncthreads();  // every window of the CTA has read its rows from d
+  if (live) f64_window(work, d, wins, wi, pool, tile, lane);
+  __syncthreads();  // every window of the CTA has stored its rows
+  bool last = false;
+  if (live) {
+    const int cc = __ldg(&wins[wi].ccount), wcount = __ldg(&wins[wi].wcount);
+    if (cc > 0 && cc < wcount) {  // the first window here of a system that other CTAs share
+      unsigned l = 0;
+      if (lane == 0) {
+        __threadfence();
+        l = atomicAdd(done + __ldg(&wins[wi].sysi), (unsigned)cc) == (unsigned)(wcount - cc);
+        if (l) __threadfence();
+      }
+      last = __shfl_sync(0xffffffffu, l, 0) != 0;
+    }
   }
-  if (!__shfl_sync(0xffffffffu, last, 0)) return;
-  border_copy(work, d, __ldg(&wins[wi].wfirst), wcount, (unsigned)lane,
-              [&](int g, long long& base, int& lo, int& blo, int& bhi, int& hi) {
-                const F64Win* v = wins + g;
-                base = __ldg(&v->off) + __ldg(&v->w0);
-                lo = __ldg(&v->lo);
-                hi = __ldg(&v->hi);
-                blo = min(__ldg(&v->blo), hi);
-                bhi = max(__ldg(&v->bhi), lo);
-              });
-  if (lane == 0) done[sysi] = 0u;
+  if (lane == 0) last_win[warp] = last ? (int)wi : -1;
+  __syncthreads();
+  for (int k = 0; k < F64W_WARPS; ++k) {
+    const int lw = last_win[k];
+    if (lw < 0) continue;
+    row_copy(work, d, border_rows + __ldg(&wins[lw].rfirst), __ldg(&wins[lw].rcount), (int)threadIdx.x,
+             32 * F64W_WARPS);
+    if (threadIdx.x == 0) done[__ldg(&wins[lw].sysi)] = 0u;
+  }
 }
 
 }  // namespace
@@ -336,12 +353,14 @@ struct Batch_ {
   long long nwin = 0;
 
   unsigned* d_done = nullptr;      // per system: its windows finished in the current launch
+  long long* d_rows = nullptr;     // the FP64 windows' border rows, grouped by system
   unsigned wpf = 0;                // the window kernel's prefetch distance (CTAs resident at once)
 
   ~Batch_() {
     if (refine) batch_refine_destroy(refine);
     if (d_wins) cudaFree(d_wins);
     if (d_done) cudaFree(d_done);
+    if (d_rows) cudaFree(d_rows);
     if (d_desc) cudaFree(d_desc);
     if (d_order) cudaFree(d_order);
     if (d_pool) cudaFree(d_pool);
@@ -550,17 +569,14 @@ bool system_windows(int n, const double* in3, const double* h6, const double* t6
     if (!cut_sequence(m, last_w0, LW / 4, pool, Kl, cl)) return false;
     add(last_w0, pos - last_w0, LW, tab, Kl, cl);
   }
-  // border rows: central rows the neighbouring windows read
+  // the system's windows; border rows are set for the whole list
+  // (ntk_batch_borders.h) once every system has its windows
   const size_t first = wins.size() - count;
   for (int g = 0; g < count; ++g) {
     F64Win& w = wins[first + g];
     w.sysi = sysi;
     w.wfirst = (int)first;
     w.wcount = count;
-    w.blo = w.lo;
-    w.bhi = w.hi;
-    if (g > 0) w.blo = std::min(w.hi, wins[first + g - 1].w0 + LW - w.w0);
-    if (g + 1 < count) w.bhi = std::max(w.lo, wins[first + g + 1].w0 - w.w0);
   }
   return true;
 }
@@ -635,6 +651,7 @@ int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long l
   // FP64: windows, one warp each, when every system admits them (else the
   // persistent one-warp-per-system kernel)
   std::vector<ntk::F64Win> wins;
+  std::vector<long long> border_rows;
   if (precision == NTK_FP64) {
     long long multi = 0;
     bool ok = true;
@@ -645,6 +662,9 @@ int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long l
     }
     if (ok) {
       b->segmented = multi;
+      ntk::cta_borders(
+          wins, ntk::F64W_WARPS, ntk::F64W_LW, [](const ntk::F64Win& w) { return w.off + w.w0; },
+          [](const ntk::F64Win& w) { return w.lo; }, [](const ntk::F64Win& w) { return w.hi; }, border_rows);
     } else {
       wins.clear();
     }
@@ -695,6 +715,13 @@ int ntk_batch_create(ntk_batch** out, long long nsys, const int* n, const long l
         rc = ntk::cuda_status(cudaMalloc(&b->d_done, sizeof(unsigned) * (size_t)nsys), "cudaMalloc(system counters)");
       if (!rc)
         rc = ntk::cuda_status(cudaMemset(b->d_done, 0, sizeof(unsigned) * (size_t)nsys), "cudaMemset(system counters)");
+      if (!rc && !border_rows.empty()) {
+        rc = ntk::cuda_status(cudaMalloc(&b->d_rows, sizeof(long long) * border_rows.size()), "cudaMalloc(border rows)");
+        if (!rc)
+          rc = ntk::cuda_status(cudaMemcpy(b->d_rows, border_rows.data(), sizeof(long long) * border_rows.size(),
+                                           cudaMemcpyHostToDevice),
+                                "cudaMemcpy(border rows)");
+      }
     }
     if (!rc && precision != NTK_FP64)
       rc = ntk::batch_refine_create(&b->refine, nsys, n, offset, interior, head, tail, precision);
@@ -767,7 +794,7 @@ int ntk_batch_solve(ntk_batch* b, double* d, void* stream) {
     // one launch: windows solved in place, border rows through work
     const long long blocks = (b->nwin + ntk::F64W_WARPS - 1) / ntk::F64W_WARPS;
     ntk::batch_f64w_kernel<<<(unsigned)blocks, 32 * ntk::F64W_WARPS, 0, st>>>(b->d_scratch, d, b->d_wins, b->nwin,
-                                                                              b->d_pool, b->d_done, b->wpf);
+                                                                              b->d_pool, b->d_rows, b->d_done, b->wpf);
     return ntk::cuda_status(cudaGetLastError(), "batch_f64w_kernel");
   }
   int rc = ntk::cuda_status(cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned), st), "cudaMemsetAsync(counter)");

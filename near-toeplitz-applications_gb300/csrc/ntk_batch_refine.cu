@@ -27,6 +27,7 @@
 #include <cmath>
 #include <vector>
 
+#include "ntk_batch_borders.h"
 #include "ntk_batch_refine.h"
 #include "ntk_r2_group.cuh"
 #include "ntk_r2_host.h"
@@ -355,26 +356,6 @@ __device__ __forceinline__ bool r2_count(const BatchWin* __restrict__ wp, unsign
     if (last) __threadfence();
   }
   return __shfl_sync(0xffffffffu, last, 0) != 0;
-}
-
-// The CTA's threads copy a system's border rows (absolute row indices in
-// rows[0, count)) from work into d, eight rows a thread in flight.
-__device__ __forceinline__ void row_copy(const double* work, double* d, const long long* __restrict__ rows,
-                                         int count, int t, int nt) {
-  for (int base = 0; base < count; base += 8 * nt) {
-    long long at[8];
-    double v[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int i = base + t + q * nt;
-      at[q] = i < count ? __ldg(rows + i) : -1;
-    }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) v[q] = at[q] >= 0 ? __ldcg(work + at[q]) : 0.0;
-#pragma unroll
-    for (int q = 0; q < 8; ++q)
-      if (at[q] >= 0) d[at[q]] = v[q];
-  }
 }
 
 // L2 prefetch of window `item`'s rows (issued by one lane): the window the
@@ -746,53 +727,11 @@ int batch_refine_create(BatchRefine** out, long long nsys, const int* n, const l
     }
   }
   for (BatchWin& w : full) w.wfirst += (int)r2w.size();
-  // Paired-chunk windows run BW to a CTA (consecutive in r2w) and every
-  // window of a CTA reads its rows before any of them stores, so only the
-  // rows a window in another CTA reads are border rows: those below the end
-  // of the last earlier window of the system in another CTA and those from
-  // the start of the first later one on (the windows' row ranges increase
-  // with their index, so these two bound every other CTA's reads; the last
-  // window can reach back past its neighbour into the window before).  The
-  // first window of a system in each CTA counts that CTA's windows of it.
-  for (size_t i = 0; i < r2w.size(); ++i) {
-    BatchWin& w = r2w[i];
-    const size_t first = (size_t)w.wfirst, last = first + (size_t)w.wcount - 1;
-    const size_t cta = i / BW;
-    const size_t cta_lo = cta * BW, cta_hi = cta_lo + BW - 1;  // this CTA's windows
-    w.blo = w.out_lo;
-    w.bhi = w.out_hi;
-    if (cta_lo > first) {  // window cta_lo - 1: the system's last window in an earlier CTA
-      const long long end = r2w[cta_lo - 1].off + BLW - w.off;
-      w.blo = (int)std::min<long long>(w.out_hi, std::max<long long>(w.out_lo, end));
-    }
-    if (cta_hi < last) {  // window cta_hi + 1: the system's first window in a later CTA
-      const long long start = r2w[cta_hi + 1].off - w.off;
-      w.bhi = (int)std::max<long long>(w.out_lo, std::min<long long>(w.out_hi, start));
-    }
-    w.ccount = 0;
-    if (i == first || (i - 1) / BW != cta) {
-      size_t e = i;
-      while (e < last && (e + 1) / BW == cta) ++e;
-      w.ccount = (int)(e - i + 1);
-    }
-  }
-  // each system's border rows (absolute indices), for the CTA that
-  // completes the system's count
+  // paired-chunk windows: border rows against other CTAs only (ntk_batch_borders.h)
   std::vector<long long> rows;
-  for (size_t i = 0; i < r2w.size();) {
-    const size_t first = i, end = i + (size_t)r2w[i].wcount;
-    const int rf = (int)rows.size();
-    for (size_t k = first; k < end; ++k) {
-      const BatchWin& w = r2w[k];
-      for (int r = w.out_lo; r < w.blo; ++r) rows.push_back(w.off + r);
-      for (int r = w.bhi; r < w.out_hi; ++r) rows.push_back(w.off + r);
-    }
-    for (size_t k = first; k < end; ++k) {
-      r2w[k].rfirst = rf;
-      r2w[k].rcount = (int)rows.size() - rf;
-    }
-    i = end;
-  }
+  cta_borders(
+      r2w, BW, BLW, [](const BatchWin& w) { return w.off; }, [](const BatchWin& w) { return w.out_lo; },
+      [](const BatchWin& w) { return w.out_hi; }, rows);
   BatchRefine* br = new (std::nothrow) BatchRefine();
   if (!br) {
     set_error("out of host memory");

@@ -134,6 +134,27 @@ __device__ __forceinline__ void border_copy(const double* work, double* d, int f
   }
 }
 
+// The nt threads of a CTA copy a system's border rows (absolute row indices
+// in rows[0, count), ntk_batch_borders.h) from work into d, eight rows a
+// thread in flight.
+__device__ __forceinline__ void row_copy(const double* work, double* d, const long long* __restrict__ rows,
+                                         int count, int t, int nt) {
+  for (int base = 0; base < count; base += 8 * nt) {
+    long long at[8];
+    double v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int i = base + t + q * nt;
+      at[q] = i < count ? __ldg(rows + i) : -1;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = at[q] >= 0 ? __ldcg(work + at[q]) : 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (at[q] >= 0) d[at[q]] = v[q];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // small utilities
 // ---------------------------------------------------------------------------
