@@ -549,7 +549,7 @@ def secondary_configs(dev, hbm):
     """The other measured workloads (rank 0, FP64 path, outside the headline):
     ADI 2048^2, r = 0.5, 100 steps replayed as one CUDA graph
     (experiments/run-adi.py:59-71); the uneven batch of 4096 systems with
-    lengths log-uniform in [32, 8192] in one persistent launch.  Each with
+    lengths log-uniform in [32, 8192] in one launch per solve.  Each with
     rows/s, HBM fraction of its algorithmic bytes, error against the oracle
     and the reference's CPU path timed on a bounded sample."""
     import time
@@ -668,8 +668,10 @@ def secondary_configs(dev, hbm):
             e1.record()
             torch.cuda.synchronize(dev)
             ms = e0.elapsed_time(e1) / reps
+            wins = bt.windows()
         ub[prec] = {"ms": ms, "rows_per_s": total_rows / (ms * 1e-3),
-                    "hbm_frac": 16.0 * total_rows / (ms * 1e-3) / 1e9 / hbm}
+                    "hbm_frac": 16.0 * total_rows / (ms * 1e-3) / 1e9 / hbm,
+                    "windows": wins["windows"], "paired_chunk_windows": wins["paired"]}
     rng = np.random.default_rng(2)
     worst = {"fp64": 0.0, "fp32_refine": 0.0}
     cpu_rows = 0
@@ -686,7 +688,8 @@ def secondary_configs(dev, hbm):
     for prec in worst:
         ub[prec]["rel_err_vs_banded_oracle_128_systems"] = worst[prec]
     ub.update({"workload": "4096 systems, lengths log-uniform in [32, 8192], 512-row windows, one warp each "
-                           "(one launch per solve in both precisions)", "rows": total_rows,
+                           "(one launch per solve in both precisions; FP32 + refine: paired-chunk windows for the "
+                           "systems of >= 512 rows)", "rows": total_rows,
                "speedup_refine_vs_fp64": ub["fp64"]["ms"] / ub["fp32_refine"]["ms"],
                "cpu_baseline": {"rows_per_s": cpu_rows / cpu_s, "cores": 1, "kind": "port",
                                 "sample": "128 systems, one scipy solve_banded each"}})
