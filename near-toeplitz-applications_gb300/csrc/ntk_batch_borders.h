@@ -54,8 +54,8 @@ void cta_borders(std::vector<WIN>& ws, int per_cta, int len, START start, LO lo,
     for (size_t k = i; k < end; ++k) {
       const WIN& w = ws[k];
       const long long s = start(w);
-      for (int r = lo(w); r < w.blo; ++r) rows.push_back(s + r);
-      for (int r = w.bhi; r < hi(w); ++r) rows.push_back(s + r);
+      for (int r = lo(w); r < hi(w); ++r)  // the two ranges can overlap: each row once
+        if (r < w.blo || r >= w.bhi) rows.push_back(s + r);
     }
     for (size_t k = i; k < end; ++k) {
       ws[k].rfirst = rf;
