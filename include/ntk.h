@@ -115,7 +115,10 @@ int ntk_plan_destroy(ntk_plan* plan);
 
 /* Status of the plan's solves since the last status read.  The FP32 and
  * FP32+refine kernels cannot represent |x| >= 2^128 (nor inf or nan) in
- * their double-word arithmetic; when a solve meets such an input it still
+ * their double-word arithmetic (and keep only FP32 accuracy for a system
+ * whose largest |x| is below about 2^-80, which is not flagged: scale such
+ * data by a power of two, which every operation preserves exactly, or use
+ * NTK_FP64); when a solve meets an input at or above 2^128 it still
  * completes, with a meaningless result, and raises NTK_STATUS_RANGE in a
  * device status word of the plan.  This call reads that word on `stream`
  * (after every solve issued before it on that stream), clears it, waits for

@@ -171,3 +171,34 @@ def test_general_coefficient_windows_match_long_double_thomas(r2emu, oracle, kin
         assert rc == 0, why.value
         ref = np.array([oracle.thomas_ld(a, b, c, row) for row in d])
         assert oracle.rel_err(out, ref) < 1e-13, (kind, ai, ci)
+
+
+def test_strong_cancellation_in_the_compact_rhs(r2emu, oracle):
+    """f = 2^20 + g with |g| ~ 1: the stencil differences f[i+1] - f[i-1]
+    cancel 20 bits of f.  They are formed in FP64 from the full values
+    (exact here), so away from the ends the derivative keeps the refinement
+    tolerance relative to its own size; rounding f to the double-word split
+    before differencing would leave ~2^-48 * 2^20 of error, far outside it.
+    The one-sided end stencils (-5 f0 + 4 f1 + f2) cancel 2^20 in any FP64
+    evaluation (the banded oracle's included); their rounding fades like
+    0.27^k into the interior, so rows 40..471 are compared."""
+    for offset in (2.0 ** 20, 2.0 ** 30):
+        f = _fourier_lines(32, 7) + offset
+        g = f - offset  # the perturbation f holds (exact)
+        ref = oracle.banded_compact_deriv(g[:, None, :], H, axis=2)[:, 0, :]
+        rc, x = r2emu_solve(r2emu, f)
+        assert rc == 0
+        assert oracle.rel_err(x[:, 40:N - 40], ref[:, 40:N - 40]) < 1e-12
+
+
+@pytest.mark.parametrize("scale", [2.0 ** 100, 2.0 ** -60])
+def test_power_of_two_scaling_is_exact(r2emu, scale):
+    """Inside the double-word range (largest |input| in [2^-80, 2^128)) every
+    operation of the solve scales exactly by a power of two: the results of
+    a scaled input are the scaled results, bit for bit."""
+    f = _fourier_lines(16, 8)
+    rc, x = r2emu_solve(r2emu, f)
+    assert rc == 0
+    rc, xs = r2emu_solve(r2emu, f * scale)
+    assert rc == 0
+    assert np.array_equal(xs, x * scale)
