@@ -3,26 +3,34 @@
 // Same windows as the ADI path (ntk_adi_refine.cu): a system longer than
 // Lw = 512 rows is cut into windows overlapping by H-row halos (H: LU
 // multiplier products below 2^-56 for the slowest-decaying system), each
-// solved by one warp with the refine kernel's machinery (refine_system) and
-// writing back only its central rows; a shorter system is one window padded
-// with identity rows.  Every system has its own coefficients, so each warp
-// builds its window's FP32 factor tables itself, lane-parallel: lane j runs
-// the pivot recurrence over its 16 rows starting from the system's converged
-// pivot carried through the two rows before its chunk (lane 0 from the
-// window's exact first row).  For these near-Toeplitz
-// matrices the pivots reach the fixed point within a few rows (the transient
-// shrinks by ~(a c / u^2) per row), so the tables are the window's FP32 LU;
-// they only precondition the refinement, whose residual uses the exact
-// double-word rows.
+// solved by one warp and writing back only its central rows; a shorter
+// system is one window padded with identity rows.  Two solves share the
+// launch:
+//  * paired-chunk windows (the full windows of every system whose window
+//    kinds qualify): the solve of ntk_r2_group.cuh with each window kind's
+//    constants (the interior Toeplitz factors and the Woodbury end
+//    corrections, prepared on the host once per batch by r2::prepare) and
+//    interior coefficients of any value in the residual (res_pair_gen);
+//  * chunked windows (short systems, and full windows of systems whose
+//    factors decay too slowly for the paired-chunk limits): the refine
+//    kernel's machinery (refine_system); every system has its own
+//    coefficients, so each warp builds its window's FP32 factor tables
+//    itself, lane-parallel: lane j runs the pivot recurrence over its 16
+//    rows starting from the system's converged pivot carried through the
+//    two rows before its chunk (lane 0 from the window's exact first row).
+//    For these near-Toeplitz matrices the pivots reach the fixed point
+//    within a few rows (the transient shrinks by ~(a c / u^2) per row), so
+//    the tables are the window's FP32 LU; they only precondition the
+//    refinement, whose residual uses the exact double-word rows.
 //
-// One launch, in place, no waiting: a window's halo rows (the rows it reads
-// but does not write) are the border rows of its neighbours (central rows
-// of theirs that it reads).  Every window reads its rows from d and writes
-// its central rows to d except its border rows, which go to the work array,
-// so d keeps every halo row unchanged while the system's windows run; each
-// window then counts itself done on its system's counter, and the window
-// that finishes last copies the system's border rows (about 2H per cut)
-// from work into d and resets the counter.
+// One launch, in place, no waiting.  A paired-chunk CTA stages its four
+// windows before a CTA barrier, so only the central rows that a window of
+// another CTA reads are border rows (ntk_batch_borders.h); they go to the
+// work array, so d keeps every row another CTA reads unchanged while the
+// system's windows run; after a second barrier the CTA counts its windows on
+// the system's counter, and the CTA that completes the count copies the
+// system's border rows from work into d and resets the counter.  Chunked
+// windows count and copy per window against both neighbours (finish_system).
 #include <algorithm>
 #include <cmath>
 #include <vector>
