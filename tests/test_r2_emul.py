@@ -202,3 +202,21 @@ def test_power_of_two_scaling_is_exact(r2emu, scale):
     rc, xs = r2emu_solve(r2emu, f * scale)
     assert rc == 0
     assert np.array_equal(xs, x * scale)
+
+
+def test_general_windows_decline_slow_decay(r2emu):
+    """With a = c = 0.45, b = 1 the multipliers (l = 0.63) decay too slowly
+    for 16-row carries even at the batch's relaxed limit (2^-22): the window
+    is declined, and the batch solves that system with the chunked kernel."""
+    import ctypes
+
+    P = ctypes.POINTER(ctypes.c_double)
+    head = np.ascontiguousarray([0., 1.5, .3, .2, 1.4, .3])
+    tail = np.ascontiguousarray([.2, 1.4, .3, .3, 1.5, 0.])
+    d = np.zeros((1, N))
+    out = np.zeros_like(d)
+    why = ctypes.create_string_buffer(256)
+    rc = r2emu.r2emu_solve_general(2, 2, head.ctypes.data_as(P), tail.ctypes.data_as(P), 0.45, 1.0, 0.45,
+                                   2.0 ** -22, 2.0 ** -22, 1, 1, d.ctypes.data_as(P), out.ctypes.data_as(P),
+                                   why, 256)
+    assert rc == 1 and b"decay" in why.value
